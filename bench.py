@@ -1,0 +1,382 @@
+"""Benchmark: 8-D Gaussian VEGAS events/s, fused fp32 vs plain float64, one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+Workload (the configuration the metric is quoted on): VegasFlow importance
+sampling of prod_d exp(-(x_d-1/2)^2/a^2)/(a sqrt(pi)), a = 0.1, n_dim = 8,
+1e8 events per iteration, 50 bins, grid refined every iteration.  One *step* is
+one full VEGAS iteration (sample -> map -> evaluate -> reduce -> refine) over
+1e8 events.  The headline ``value`` is the fused fp32 form (in-kernel Philox
+uniforms, fp32 map/evaluation, compensated sums, float64 across blocks); the
+plain float64 path runs the same steps and is reported beside it with both
+sigmas (the metric compares them at equal sigma).
+
+Timing: W untimed warm-up iterations, then K timed iterations, each bracketed by
+CUDA events on the launching stream; between timed iterations the L2 is flushed
+by writing a 512 MB buffer (outside the timed windows).  The iterations draw no
+HBM inputs (uniforms come from the in-kernel Philox stream).  Under torchrun
+(N > 1) every rank runs an independent replica (different seed), the reported
+value is the events of all ranks divided by the slowest rank's time.
+
+``--impl reference`` times the reference algorithm's CPU restatement (the
+oracle: TensorFlow is not available on the host) on all host threads, over a
+bounded sample of the same workload per step.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "8-D Gaussian events/s, fused FP32 vs plain FP64 at equal σ; served p50/p99"
+N_DIM = 8
+A_WIDTH = 0.1
+EVENTS = 100_000_000
+L2_FLUSH_BYTES = 512 << 20
+
+# Algorithmic instruction budget of one event of the fused fp32 sampler at
+# n_dim = 8 (VEGAS map, Gaussian, compensated sums, histogram): counted from the
+# algorithm, not from the compiled kernel.
+#   Philox4x32-10: 2 blocks x (10 rounds x (2 wide multiplies + 2 three-input xors) + 2)  84
+#   map, per dim: not+multiply-add (2), fraction bits (2), fadd, grid load + address (2),
+#                 fma (x), fmul (w)                                        9 x 8 =   72
+#   Gaussian: 2 fma per dim (16), exp2 (2), prefactor (1)                              19
+#   w f, (w f)^2, two TwoSum accumulations (12)                                        14
+#   histogram: address + shared atomic per dim                             2 x 8 =   16
+#   loop control                                                                        3
+INSTR_PER_EVENT_FP32_D8 = 208
+
+
+def _parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--events", type=int, default=EVENTS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ distributed
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(value, world):
+    """The slowest rank's time (replicas: max over ranks)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ reference arm
+def cpu_oracle_rate(n_events, threads, seed=0):
+    """One float64 VegasFlow iteration of the 8-D Gaussian on the host (the
+    oracle restatement of the reference), on `threads` threads."""
+    import numpy as np
+
+    import oracle
+
+    grid = oracle.initial_grid(N_DIM)
+    t0 = time.perf_counter()
+    res, sigma, arr = oracle.threaded_vegas_iteration(
+        grid, n_events, lambda x: oracle.integrand_symgauss(x, A_WIDTH), seed, threads)
+    dt = time.perf_counter() - t0
+    _ = oracle.refine_grid(arr, grid)
+    return n_events / dt, dt, res, sigma
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = host_threads()
+    sample = 4_000_000
+    for _ in range(max(0, args.warmup)):
+        cpu_oracle_rate(1_000_000, threads)
+    rates, times = [], []
+    for k in range(args.steps):
+        r, dt, _, _ = cpu_oracle_rate(sample, threads, seed=k)
+        rates.append(r)
+        times.append(dt)
+    value = sample * len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (NumPy PCG64 uniforms through the TECH_CUT affine)",
+        "config": workload_config(args, sample_events=sample),
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} iterations x {sample:.0e} events of the 8-D Gaussian, "
+                                   "float64 VegasFlow oracle, NumPy on host threads"},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, sample_events=None):
+    cfg = {"workload": "8-D Gaussian a=0.1, VegasFlow importance sampling (grid trained every "
+                       "iteration), 50 bins, 1e8 events/iteration",
+           "n_dim": N_DIM, "events_per_iteration": args.events, "bins": 50,
+           "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
+           "l2": "no HBM inputs (in-kernel Philox); L2 flushed (512 MB write) between timed iterations"}
+    if sample_events:
+        cfg["sample_events_per_step"] = sample_events
+    return cfg
+
+
+# ------------------------------------------------------------------ GPU arm
+def main():
+    args = _parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import numpy as np
+    import torch
+
+    from vegasflow_gb300 import VegasFlow, integrands
+    from vegasflow_gb300 import _native as nat
+    from vegasflow_gb300.build import build
+
+    build()
+    assert torch.cuda.is_available(), "bench.py needs a CUDA GPU"
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    exact = math.erf(0.5 / A_WIDTH) ** N_DIM
+    K, W = args.steps, max(3, args.warmup)
+
+    def timed_run(precision, seed):
+        """W warm-up + K timed iterations; returns per-iteration and sampler times (s)."""
+        inst = VegasFlow(N_DIM, args.events, verbose=False, precision=precision, seed=seed, device=dev)
+        inst.compile(integrands.symgauss(A_WIDTH))
+        for _ in range(W):
+            inst._run_iteration()
+        inst._reset_average()
+        torch.cuda.synchronize()
+        barrier(world)
+        step_ms, samp_ms = [], []
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+               torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        for k in range(K):
+            flush.fill_(float(k))
+            a, b, c = ev[k]
+            a.record(stream)
+            inst._fill_partials(train=inst.train)
+            b.record(stream)
+            inst._end_iteration(train=inst.train)
+            c.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        for a, b, c in ev:
+            step_ms.append(a.elapsed_time(c))
+            samp_ms.append(a.elapsed_time(b))
+        hist = inst._workspace()["history"][:K].cpu().numpy()
+        avg = inst._workspace()["avg"].cpu().numpy()
+        return inst, np.array(step_ms) / 1e3, np.array(samp_ms) / 1e3, hist, avg
+
+    with ClockSampler(local) as clocks:
+        inst32, t32, s32, h32, a32 = timed_run("fp32", seed=2 + 1000 * rank)
+        inst64, t64, s64, h64, a64 = timed_run("fp64", seed=3 + 1000 * rank)
+
+        # issue-rate calibration at the same clocks
+        probe_blocks = 152 * 8
+        probe_buf = torch.empty(probe_blocks * 256, dtype=torch.float32, device=dev)
+        import ctypes
+        fpt = ctypes.c_longlong(0)
+        lib = nat.load()
+        for _ in range(2):
+            nat.check(lib.vf_issue_probe(nat.ptr(probe_buf), probe_blocks, 4000, ctypes.byref(fpt),
+                                         nat.stream_handle()))
+        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pa.record(stream)
+        nat.check(lib.vf_issue_probe(nat.ptr(probe_buf), probe_blocks, 4000, ctypes.byref(fpt),
+                                     nat.stream_handle()))
+        pb.record(stream)
+        torch.cuda.synchronize()
+        probe_s = pa.elapsed_time(pb) / 1e3
+        issue_peak = probe_blocks * 256 * fpt.value / 32 / probe_s  # warp instructions / s
+
+        # end-to-end through the public API with a host-resident grid
+        e2e = e2e_run(inst32, K, dev)
+    clk = clocks.summary()
+
+    total32 = float(t32.sum())
+    total32 = max_over_ranks(total32, world)
+    total64 = max_over_ranks(float(t64.sum()), world)
+    events_all = args.events * K * world
+    value = events_all / total32
+    value64 = events_all / total64
+
+    samp_mean = float(s32.mean())
+    achieved = INSTR_PER_EVENT_FP32_D8 * args.events / 32 / samp_mean  # warp instr / s
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": 1e3 * total32 / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (in-kernel Philox4x32-10 uniforms)",
+        "config": workload_config(args),
+        "result": {"fp32": {"mean": float(a32[2]), "sigma": float(a32[3]), "chi2_dof": float(a32[4]),
+                            "pull_vs_exact": (float(a32[2]) - exact) / float(a32[3])},
+                   "fp64": {"mean": float(a64[2]), "sigma": float(a64[3]), "chi2_dof": float(a64[4]),
+                            "pull_vs_exact": (float(a64[2]) - exact) / float(a64[3])},
+                   "exact": exact},
+        "fp64_plain": {"value": value64, "unit": "events/s", "ms_per_step": 1e3 * total64 / K,
+                       "sampler_ms": 1e3 * float(s64.mean())},
+        "fp32_over_fp64": value / value64,
+        "roofline": {"bound": "issue", "kernel": "vf_sample_kernel<float,8,SYMGAUSS>",
+                     "achieved": achieved / 1e9, "peak": issue_peak / 1e9, "unit": "Gwarp-instr/s",
+                     "frac": achieved / issue_peak, "traffic": None,
+                     "per_event_instr": INSTR_PER_EVENT_FP32_D8,
+                     "peak_source": "measured in this run: vf_issue_probe (independent FFMA chains)",
+                     "sampler_ms": 1e3 * samp_mean},
+        "e2e": e2e,
+        "gpu_launches": 2 * K,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = host_threads()
+        cpu_oracle_rate(500_000, threads)
+        rate, dt, _, _ = cpu_oracle_rate(8_000_000, threads, seed=1)
+        line["cpu_baseline"] = {"value": rate, "unit": "events/s", "cores": threads, "kind": "port",
+                                "sample": "1 iteration x 8e6 events of the 8-D Gaussian, float64 "
+                                          "VegasFlow oracle (NumPy) on the host threads",
+                                "seconds": dt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def e2e_run(inst, K, dev):
+    """K steps through the public API (``run_integration(1)`` per step) with the
+    grid kept in pinned host memory: per step H2D of the grid, the iteration and
+    the D2H read of its (result, sigma), then D2H of the refined grid."""
+    import torch
+
+    host_grid = inst.divisions.cpu().pin_memory()
+    for _ in range(2):
+        inst.divisions.copy_(host_grid, non_blocking=True)
+        inst.run_integration(1)
+        host_grid.copy_(inst.divisions, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        inst.divisions.copy_(host_grid, non_blocking=True)
+        inst.run_integration(1)
+        host_grid.copy_(inst.divisions, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    dt = time.perf_counter() - t0
+    nbytes = host_grid.numel() * 8
+    return {"value": inst.n_events * K / dt, "unit": "events/s", "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes + 16 + 5 * 8 + 8,
+            "api": "VegasFlow.run_integration(1) per step, grid resident in pinned host memory"}
+
+
+if __name__ == "__main__":
+    main()

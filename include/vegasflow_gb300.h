@@ -1,0 +1,140 @@
+/*
+ * vegasflow_gb300 -- C-ABI of the GB300 (sm_103a) VEGAS hot path.
+ *
+ * libvegasgb.so exports the entry points below.  Every buffer argument is a
+ * caller-owned device pointer (plain pointers and sizes, no framework types);
+ * `stream` is a cudaStream_t (NULL = the legacy default stream).  No entry point
+ * allocates device memory or synchronises the stream, except vf_jit_integrand
+ * (host-side compilation and module load).  Every call returns VF_OK (0) or a
+ * VF_ERR_* code; vf_last_error_string() describes the last failure of the
+ * calling thread.  Calls are thread-safe; work on one stream is ordered.
+ *
+ * Reference interfaces (N3PDF/vegasflow 1.4.0, paths inside that project) are
+ * cited per entry point: each C function replaces the TensorFlow graph the
+ * reference compiles for that step.
+ */
+#ifndef VEGASFLOW_GB300_H
+#define VEGASFLOW_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define VF_OK 0
+#define VF_ERR_ARG 1          /* invalid argument (pointer, size, mode)          */
+#define VF_ERR_LAUNCH 2       /* a kernel launch failed                          */
+#define VF_ERR_TIMEOUT 3      /* a bounded device-side wait gave up              */
+#define VF_ERR_NONFINITE 4    /* a result was NaN/Inf                            */
+#define VF_ERR_JIT 5          /* NVRTC compilation or module load failed         */
+#define VF_ERR_CUDA 6         /* a CUDA runtime call failed                      */
+#define VF_ERR_UNSUPPORTED 7  /* configuration not built (e.g. n_dim > 16)       */
+
+/* ---- device error flags (bit set in the optional `flags` word) ------------ */
+#define VF_FLAG_INDEX_RANGE 1     /* a uniform mapped outside the grid (clamped)  */
+#define VF_FLAG_REFINE_OVERRUN 2  /* the rebinning walk ran past the last bin     */
+#define VF_FLAG_NONFINITE 4       /* a partial sum was NaN or Inf                 */
+
+/* ---- constants (configflow.py:13-24) -------------------------------------- */
+#define VF_BINS_MAX 50
+#define VF_MAX_DIM 16
+
+/* ---- algorithms / precisions ---------------------------------------------- */
+#define VF_ALG_VEGAS 0  /* importance sampling, vflow.py:215                     */
+#define VF_ALG_PLAIN 1  /* plain MC, plain.py:11                                 */
+#define VF_PREC_F64 0   /* the reference's float64 arithmetic                    */
+#define VF_PREC_F32 1   /* fused fp32 form, compensated sums, float64 across blocks */
+
+/* ---- built-in integrands (parameters are a float64 device array) --------- */
+#define VF_INT_NONE 0          /* sample only (x, w, ind taps)                   */
+#define VF_INT_SYMGAUSS 1      /* {a, (1/(a sqrt(pi)))^D}                        */
+#define VF_INT_GAUSS 2         /* {mu[D], a[D]}                                  */
+#define VF_INT_BREIT_WIGNER 3  /* {M, Gamma, c[D-1]}                             */
+#define VF_INT_PROD 4          /* none                                           */
+#define VF_INT_SUM 5           /* none                                           */
+#define VF_INT_JIT_BASE 1000   /* ids returned by vf_jit_integrand               */
+
+int vf_version(void);
+const char* vf_last_error_string(void);
+/* SM count and compute capability of the current device. */
+int vf_device_info(int* sm_count, int* cc_major, int* cc_minor);
+
+/*
+ * Number of per-block partial rows (= blocks of the persistent grid) the
+ * sampler uses for this configuration.  The caller sizes `partials` as
+ * rows * (2 + 50 * n_dim) doubles.
+ */
+int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, int* rows);
+
+/*
+ * One chunk of events through the fused sampler.  Replaces the compiled
+ * `self.event` of MonteCarloFlow.compile (monte_carlo.py:593-600), i.e.
+ * VegasFlow._run_event (vflow.py:389-430) = _generate_random_array
+ * (monte_carlo.py:249-275, vflow.py:93-126, importance_sampling_digest
+ * vflow.py:39-83) + integrand + reductions + _importance_sampling_array_filling
+ * (vflow.py:370-387), and PlainFlow._run_event (plain.py:18-35).
+ *
+ *  grid      [n_dim][51] bin edges (VEGAS only)
+ *  xjac      1 / events per iteration (monte_carlo.py:225-227)
+ *  xmin, xdelta  nullable [n_dim] integration limits, xdeltajac = prod(xdelta)
+ *  u_inj     nullable [n_events][n_dim] injected uniforms (post TECH_CUT affine);
+ *            NULL = in-kernel Philox4x32-10 keyed by `seed`, counter (event
+ *            ev_offset+i, call_ctr)
+ *  integrand VF_INT_* or a JIT id; params its float64 parameters
+ *  train     fill the per-bin histogram of (w f)^2
+ *  partials  [rows][2 + 50 n_dim] block partials: stored (accumulate=0) or added
+ *  ind_out, x_out, w_out, f_out  nullable per-event taps ([n][D] int32,
+ *            [n][D] / [n] / [n] in the precision's type)
+ *  flags     nullable device int receiving VF_FLAG_* bits
+ */
+int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n_events,
+              long long ev_offset, double xjac, const double* xmin, const double* xdelta,
+              double xdeltajac, const double* u_inj, unsigned long long seed,
+              unsigned int call_ctr, int integrand, const double* params, int train,
+              int accumulate, double* partials, int rows, int* ind_out, void* x_out,
+              void* w_out, void* f_out, int* flags, void* stream);
+
+/*
+ * Partial rows from integrand values produced outside the sampler (a torch
+ * callable evaluated on the sampler's x): tmp = w f, sums of tmp and tmp^2 per
+ * output, histogram of the `main_dim` output.  Replaces vflow.py:414-428 /
+ * plain.py:310-317 for integrands that are not device functions; `n_out` > 1 is
+ * the vectorial case (vflow.py:245-252).
+ */
+int vf_reduce_events(int precision, const void* f, const void* w, const int* ind,
+                     long long n_events, int n_dim, int n_out, int main_dim, int train,
+                     int accumulate, double* partials, int rows, int* flags, void* stream);
+
+/*
+ * Iteration end: fixed-order sum of the partial rows, sigma
+ * (vflow.py:437-438), history[iter] = (res, sigma), the running
+ * 1/sigma^2-weighted mean, its sigma and chi^2/dof in avg[n_out][5]
+ * (monte_carlo.py:712-732), and -- when train -- refine_grid (vflow.py:349-362,
+ * refine_grid_per_dimension vflow.py:135-211) on `grid` in place.
+ */
+int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int train,
+                     double n_events, double alpha, double* grid, double* hist_out,
+                     double* sums_out, double* history, double* avg, int iter, int* flags,
+                     void* stream);
+
+/* VegasFlow.refine_grid(arr_res2) (vflow.py:349-362): hist [n_dim][50]. */
+int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, int* flags,
+                   void* stream);
+
+/* consume_array_into_indices (utils.py:17-44): out[size] = per-bin sums. */
+int vf_consume_array_into_indices(const double* input, const int* indices, long long n,
+                                  int result_size, double* out, int* flags, void* stream);
+
+/*
+ * Calibration (no counterpart in the reference): `blocks` x 256 threads each
+ * issue 128 * iters independent fp32 FMAs, so the kernel's duration gives the
+ * achievable warp-instruction issue rate, the roofline of the compute-bound
+ * fused sampler.  `out` is a device buffer of blocks * 256 floats (written only
+ * on an impossible value); *fma_per_thread receives 128 * iters.
+ */
+int vf_issue_probe(float* out, int blocks, int iters, long long* fma_per_thread, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VEGASFLOW_GB300_H */

@@ -1,0 +1,134 @@
+"""Host-side logic that needs no GPU: constructor validation, grid JSON I/O,
+configuration, and the refusal to compute without CUDA (no CPU fallback)."""
+
+import json
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from vegasflow_gb300 import PlainFlow, VegasFlow, configflow, float_me, int_me, integrands
+
+
+def test_integration_limits_checks():
+    """test_misc.py:85-97."""
+    with pytest.raises(ValueError):
+        PlainFlow(1, 10, xmin=[10], xmax=[1], device="cpu")
+    with pytest.raises(ValueError):
+        PlainFlow(1, 10, xmin=[10], device="cpu")
+    with pytest.raises(ValueError):
+        PlainFlow(1, 10, xmax=[10], device="cpu")
+    with pytest.raises(ValueError):
+        PlainFlow(2, 10, xmin=[0], xmax=[1], device="cpu")
+    with pytest.raises(ValueError):
+        PlainFlow(2, 10, xmin=[0, 1], xmax=[1], device="cpu")
+
+
+def test_dimension_and_precision_validation():
+    with pytest.raises(ValueError):
+        VegasFlow(17, 100, device="cpu")
+    with pytest.raises(ValueError):
+        VegasFlow(0, 100, device="cpu")
+    with pytest.raises(ValueError):
+        VegasFlow(2, 100, precision="fp16", device="cpu")
+
+
+def test_initial_grid_matches_reference():
+    inst = VegasFlow(3, 100, device="cpu")
+    np.testing.assert_array_equal(inst.divisions.numpy(), oracle.initial_grid(3))
+    assert inst.grid_bins == 51
+
+
+def test_save_and_load_grid_json(tmp_path):
+    """test_algs.py:102-148 on the host side: JSON round trip and the errors."""
+    inst = VegasFlow(2, 100, device="cpu")
+    grid = np.sort(np.random.default_rng(0).random((2, 51)), axis=1)
+    inst.load_grid(numpy_grid=grid)
+    np.testing.assert_array_equal(inst.divisions.numpy(), grid)
+    fname = tmp_path / "grid.json"
+    inst.save_grid(str(fname))
+    d = json.load(open(fname))
+    assert set(d) == {"dimensions", "ALPHA", "BINS", "integrand", "grid"}
+    assert d["dimensions"] == 2 and d["BINS"] == 51 and d["ALPHA"] == 1.5
+    np.testing.assert_array_equal(np.array(d["grid"]), grid)
+    other = VegasFlow(2, 100, device="cpu")
+    other.load_grid(file_name=str(fname))
+    np.testing.assert_array_equal(other.divisions.numpy(), grid)
+    jdict = {"grid": grid.tolist(), "BINS": 0}
+    json.dump(jdict, open(fname, "w"))
+    with pytest.raises(ValueError):
+        other.load_grid(file_name=str(fname))
+    jdict["dimensions"] = -4
+    json.dump(jdict, open(fname, "w"))
+    with pytest.raises(ValueError):
+        other.load_grid(file_name=str(fname))
+    with pytest.raises(ValueError):
+        other.load_grid(file_name=str(fname), numpy_grid=grid)
+    with pytest.raises(ValueError):
+        other.load_grid()
+
+
+def test_no_cpu_fallback():
+    inst = VegasFlow(2, 1000, device="cpu", verbose=False)
+    inst.compile(integrands.symgauss())
+    with pytest.raises(RuntimeError, match="CUDA"):
+        inst.run_integration(1)
+
+
+def test_compile_requires_callable():
+    inst = VegasFlow(2, 100, device="cpu")
+    with pytest.raises(TypeError):
+        inst.compile(42)
+
+
+def test_run_before_compile_raises():
+    inst = PlainFlow(2, 100, device="cpu")
+    with pytest.raises(RuntimeError):
+        inst._recompile()
+
+
+def test_casts_and_dtypes():
+    """test_config.py:11-19."""
+    assert int_me(4).dtype == configflow.DTYPEINT
+    assert float_me(4.0).dtype == configflow.DTYPE
+    assert configflow.DTYPE == torch.float64 and configflow.DTYPEINT == torch.int32
+
+
+def test_float_env(monkeypatch):
+    """test_config.py:22-53: VEGASFLOW_FLOAT / VEGASFLOW_INT select the dtypes."""
+    import importlib
+    monkeypatch.setenv("VEGASFLOW_FLOAT", "32")
+    monkeypatch.setenv("VEGASFLOW_INT", "64")
+    mod = importlib.reload(configflow)
+    try:
+        assert mod.DTYPE == torch.float32 and mod.DTYPEINT == torch.int64
+        assert mod.DEFAULT_PRECISION == "fp32"
+    finally:
+        monkeypatch.delenv("VEGASFLOW_FLOAT")
+        monkeypatch.delenv("VEGASFLOW_INT")
+        importlib.reload(configflow)
+
+
+def test_integrand_params():
+    p = integrands.symgauss(0.1).params(4)
+    assert p[0] == 0.1 and abs(p[1] - (1 / 0.1 / np.sqrt(np.pi)) ** 4) < 1e-9
+    g = integrands.gauss([0.4, 0.6], [0.1, 0.2])
+    np.testing.assert_array_equal(g.params(2), [0.4, 0.6, 0.1, 0.2])
+    with pytest.raises(ValueError):
+        g.check_dims(3)
+    bw = integrands.breit_wigner([0.1, 0.2, 0.3])
+    np.testing.assert_array_equal(bw.params(4), [91.19, 2.5, 0.1, 0.2, 0.3])
+    with pytest.raises(ValueError):
+        bw.params(6)
+
+
+def test_integrand_torch_forms_match_oracle():
+    x = np.random.default_rng(1).random((100, 3))
+    t = torch.as_tensor(x)
+    np.testing.assert_allclose(integrands.symgauss(0.1)(t).numpy(), oracle.integrand_symgauss(x, 0.1),
+                               rtol=1e-13)
+    c = [0.3, 0.7]
+    np.testing.assert_allclose(integrands.breit_wigner(c)(t).numpy(),
+                               oracle.integrand_breit_wigner(x, coeffs=c), rtol=1e-13)
+    np.testing.assert_allclose(integrands.prod()(t).numpy(), oracle.integrand_prod(x), rtol=1e-15)

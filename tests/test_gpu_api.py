@@ -1,0 +1,227 @@
+"""The reference's own test suite (src/vegasflow/tests), ported to this API.
+
+Same integrands, sizes and acceptance (3 sigma / 5 sigma / exact), run on the
+GPU through the public classes.  Torch callables play the role of the
+reference's TensorFlow integrands; device integrands are exercised too."""
+
+import json
+
+import numpy as np
+import pytest
+import torch
+
+from vegasflow_gb300 import (PlainFlow, VegasFlow, integrands, plain_sampler, plain_wrapper,
+                             vegas_sampler, vegas_wrapper)
+
+pytestmark = pytest.mark.gpu
+
+dim = 2
+ncalls = np.int32(1e4)
+n_iter = 4
+
+
+def example_integrand(xarr, weight=None):
+    """test_algs.py:27-36, in torch."""
+    n_dim = xarr.shape[-1]
+    a = 0.1
+    n100 = float(100 * n_dim)
+    pref = (1.0 / a / np.sqrt(np.pi)) ** n_dim
+    coef = torch.sum(torch.arange(n100 + 1, dtype=xarr.dtype, device=xarr.device))
+    coef = coef + torch.sum(((xarr - 0.5) / a) ** 2, dim=1)
+    coef = coef - (n100 + 1) * n100 / 2.0
+    return pref * torch.exp(-coef)
+
+
+def instance_and_compile(Integrator, mode=0, integrand_function=example_integrand, **kw):
+    """test_algs.py:39-60 (signature modes 0-3)."""
+    if mode == 0:
+        integrand = integrand_function
+    elif mode == 1:
+        def integrand(xarr, n_dim=None):
+            return integrand_function(xarr)
+    elif mode == 2:
+        def integrand(xarr):
+            return integrand_function(xarr)
+    elif mode == 3:
+        def integrand(xarr, n_dim=None, weight=None):
+            return integrand_function(xarr, weight=None)
+    int_instance = Integrator(dim, ncalls, verbose=False, **kw)
+    int_instance.compile(integrand)
+    return int_instance
+
+
+def check_is_one(result, sigmas=3, target_result=1.0):
+    """test_algs.py:63-68."""
+    res = result[0]
+    err = np.mean(result[1] * sigmas)
+    np.testing.assert_allclose(res, target_result, atol=err)
+
+
+@pytest.mark.parametrize("mode", range(4))
+def test_VegasFlow(mode):
+    vegas_instance = instance_and_compile(VegasFlow, mode)
+    _ = vegas_instance.run_integration(n_iter)
+    vegas_instance.freeze_grid()
+    result = vegas_instance.run_integration(n_iter)
+    check_is_one(result)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_VegasFlow_device_integrand(precision):
+    inst = VegasFlow(dim, ncalls, verbose=False, precision=precision)
+    inst.compile(integrands.symgauss())
+    _ = inst.run_integration(n_iter)
+    inst.freeze_grid()
+    check_is_one(inst.run_integration(n_iter))
+
+
+def test_VegasFlow_grid_management():
+    vegas_instance = instance_and_compile(VegasFlow, 1)
+    _ = vegas_instance.run_integration(n_iter)
+    vegas_instance.freeze_grid()
+    vegas_instance.n_events = 2 * ncalls
+    check_is_one(vegas_instance.run_integration(n_iter))
+    vegas_instance.unfreeze_grid()
+    check_is_one(vegas_instance.run_integration(n_iter))
+    vegas_instance.n_events = 3 * ncalls
+    check_is_one(vegas_instance.run_integration(n_iter))
+
+
+def test_VegasFlow_save_grid(tmp_path):
+    fname = str(tmp_path / "grid.json")
+    vegas_instance = instance_and_compile(VegasFlow)
+    _ = vegas_instance.run_integration(1)
+    current_grid = vegas_instance.divisions.cpu().numpy()
+    vegas_instance.save_grid(fname)
+    with open(fname) as f:
+        json_grid = np.array(json.load(f)["grid"])
+    np.testing.assert_equal(current_grid, json_grid)
+
+
+def test_VegasFlow_load_grid(tmp_path):
+    fname = str(tmp_path / "grid.json")
+    vegas_instance = instance_and_compile(VegasFlow)
+    grid_shape = tuple(vegas_instance.divisions.shape)
+    tmp_grid = np.random.rand(*grid_shape)
+    with open(fname, "w") as f:
+        json.dump({"grid": tmp_grid.tolist()}, f)
+    vegas_instance.load_grid(file_name=fname)
+    np.testing.assert_equal(vegas_instance.divisions.cpu().numpy(), tmp_grid)
+    tmp_grid = np.random.rand(*grid_shape)
+    vegas_instance.load_grid(numpy_grid=tmp_grid)
+    np.testing.assert_equal(vegas_instance.divisions.cpu().numpy(), tmp_grid)
+
+
+@pytest.mark.parametrize("mode", range(4))
+def test_PlainFlow(mode):
+    check_is_one(instance_and_compile(PlainFlow, mode).run_integration(n_iter))
+
+
+def test_PlainFlow_change_nevents():
+    plain_instance = instance_and_compile(PlainFlow, 0)
+    check_is_one(plain_instance.run_integration(n_iter))
+    plain_instance.n_events = 2 * ncalls
+    check_is_one(plain_instance.run_integration(n_iter))
+
+
+def helper_rng_tester(sampling_function, n_events):
+    rnds, px = sampling_function(n_events)
+    np.testing.assert_equal(tuple(rnds.shape), (n_events, dim))
+    return rnds, px
+
+
+def test_rng_generation_plain(n_events=100):
+    plain_sampler_instance = instance_and_compile(PlainFlow)
+    _, px = helper_rng_tester(plain_sampler_instance.generate_random_array, n_events)
+    np.testing.assert_equal(px.cpu().numpy(), 1.0 / n_events)
+
+
+def test_rng_generation_vegasflow(n_events=100):
+    vegas_sampler_instance = instance_and_compile(VegasFlow)
+    vegas_sampler_instance.run_integration(2)
+    _, px = helper_rng_tester(vegas_sampler_instance.generate_random_array, n_events)
+    np.testing.assert_equal(tuple(px.shape), (n_events,))
+
+
+def test_rng_generation_wrappers(n_events=100):
+    p = plain_sampler(example_integrand, dim, n_events, training_steps=2, return_class=True)
+    _ = helper_rng_tester(p.generate_random_array, n_events)
+    v = vegas_sampler(example_integrand, dim, n_events, training_steps=2)
+    _ = helper_rng_tester(v, n_events)
+
+
+def test_wrappers():
+    check_is_one(vegas_wrapper(integrands.symgauss(), 4, 5, int(1e5)))
+    check_is_one(plain_wrapper(integrands.symgauss(), 1, 3, int(1e5)))
+
+
+# ---- test_misc.py
+def _vector_integrand(xarr, weight=None):
+    res = ((xarr - 1.0) ** 2) ** 2
+    return torch.exp(-res) / 0.845
+
+
+def _wrong_integrand(xarr):
+    return torch.sum(xarr)
+
+
+def _simple_integral(xmin, xmax):
+    xm = np.array(xmin) ** 2 / 2.0
+    xp = np.array(xmax) ** 2 / 2.0
+    return np.prod(xp - xm)
+
+
+def _wrong_vector_integrand(xarr):
+    return xarr.T
+
+
+@pytest.mark.parametrize("mode", range(4))
+@pytest.mark.parametrize("alg", [VegasFlow, PlainFlow])
+def test_working_vectorial(alg, mode):
+    inst = instance_and_compile(alg, mode=mode, integrand_function=_vector_integrand)
+    result = inst.run_integration(2)
+    check_is_one(result, sigmas=5)
+
+
+def test_check_wrong_main_dimension():
+    inst = VegasFlow(3, 100, main_dimension=5, verbose=False)
+    with pytest.raises(ValueError):
+        inst.compile(_vector_integrand)
+
+
+@pytest.mark.parametrize("wrong_fun", [_wrong_vector_integrand, _wrong_integrand])
+def test_wrong_shape(wrong_fun):
+    with pytest.raises(ValueError):
+        _ = instance_and_compile(PlainFlow, integrand_function=wrong_fun)
+
+
+@pytest.mark.parametrize("alg", [PlainFlow, VegasFlow])
+@pytest.mark.parametrize("kind", ["torch", "device"])
+def test_integration_limits(alg, kind, ncalls=int(1e4)):
+    rng = np.random.default_rng(17)
+    dims = int(rng.integers(1, 5))
+    xmin = -1.0 + rng.random(dims) * 2.0
+    xmax = 3.0 + rng.random(dims)
+    inst = alg(dims, ncalls, xmin=xmin, xmax=xmax, verbose=False)
+    inst.compile(integrands.prod() if kind == "device" else (lambda x: torch.prod(x, dim=1)))
+    result = inst.run_integration(5)
+    check_is_one(result, target_result=_simple_integral(xmin, xmax))
+
+
+def test_history_and_chi2():
+    inst = VegasFlow(4, 100_000, verbose=False, seed=5)
+    inst.compile(integrands.symgauss())
+    res, sig = inst.run_integration(5)
+    assert len(inst.history) == 5
+    assert all(len(h) == 3 for h in inst.history)
+    assert 0.0 <= inst.chi2_dof < 10.0
+    check_is_one((res, sig))
+
+
+def test_seed_reproducible():
+    out = []
+    for _ in range(2):
+        inst = VegasFlow(3, 100_000, verbose=False, seed=42)
+        inst.compile(integrands.symgauss())
+        out.append(inst.run_integration(3))
+    np.testing.assert_allclose(out[0], out[1], rtol=1e-12)

@@ -1,0 +1,113 @@
+"""Build libvegasgb.so (the CUDA kernels + C-ABI) for sm_103a with nvcc.
+
+    python -m vegasflow_gb300.build [--force] [-v]
+
+Each ``csrc/*.cu`` / ``*.cpp`` is compiled in parallel to an object file under
+``vegasflow_gb300/_build/``, then linked into ``_build/libvegasgb.so``.  Objects
+are rebuilt when any source or header is newer.  No CMake, one -gencode.
+"""
+
+from __future__ import annotations
+
+import argparse
+import glob
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(BUILD, "libvegasgb.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              f"-I{INCLUDE}", f"-I{CSRC}"]
+
+
+def nvcc_path():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA 13 toolkit is required to build vegasflow_gb300")
+
+
+def cuda_home():
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc_path())))
+
+
+def _sources():
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+
+
+def _headers():
+    return (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+            + glob.glob(os.path.join(INCLUDE, "*.h")))
+
+
+def _newest(paths):
+    return max((os.path.getmtime(p) for p in paths), default=0.0)
+
+
+def _compile(src, obj, verbose, extra):
+    cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+    if src.endswith(".cpp"):
+        cmd[1:1] = ["-x", "cu"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout + r.stderr, flush=True)
+    return obj
+
+
+def build(force=False, verbose=False, jobs=None, extra_flags=()):
+    """Compile and link libvegasgb.so; returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = _sources()
+    hdr_time = _newest(_headers())
+    todo = []
+    objs = []
+    for s in srcs:
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(s))[0] + ".o")
+        objs.append(obj)
+        if force or not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(s), hdr_time):
+            todo.append((s, obj))
+    jobs = jobs or min(len(todo) or 1, os.cpu_count() or 4)
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        list(ex.map(lambda so: _compile(so[0], so[1], verbose, list(extra_flags)), todo))
+    if force or todo or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
+        home = cuda_home()
+        lib64 = os.path.join(home, "lib64")
+        cmd = [nvcc_path(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs,
+               f"-L{lib64}", "-lcudart", "-lnvrtc", "-lcuda", f"-L{os.path.join(lib64, 'stubs')}",
+               "-Xlinker", f"-rpath={lib64}"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("-v", "--verbose", action="store_true")
+    ap.add_argument("--ptxas-info", action="store_true", help="print -Xptxas -v register/smem usage")
+    args = ap.parse_args(argv)
+    extra = ["-Xptxas", "-v"] if args.ptxas_info else []
+    path = build(force=args.force or args.ptxas_info, verbose=args.verbose or args.ptxas_info,
+                 extra_flags=extra)
+    print(path)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,246 @@
+// The extern "C" entry points of libvegasgb.so (declared in
+// include/vegasflow_gb300.h): argument checks, kernel selection, launch.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "vegasflow_gb300.h"
+#include "vf_internal.h"
+#include "vf_iter.cuh"
+#include "vf_sample.cuh"
+
+namespace {
+
+thread_local char g_err[1024] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int check_launch(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "%s: %s", what, cudaGetErrorString(e));
+  return VF_OK;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  return n;
+}
+
+bool builtin_integrand(int id) { return id >= VF_INT_NONE && id <= VF_INT_SUM; }
+
+// Per-warp histogram copies for fp32 (fewer same-address collisions), one block
+// copy for float64 (shared float64 atomics, smem budget).
+int hist_copies_for(int precision) { return precision == VF_PREC_F32 ? VF_THREADS / 32 : 1; }
+
+const void* sample_kernel(int precision, int n_dim, int integrand) {
+  const int dmax = vf::dim_bucket(n_dim);
+  return precision == VF_PREC_F64 ? vf::sample_kernel_f64(dmax, integrand)
+                                  : vf::sample_kernel_f32(dmax, integrand);
+}
+
+int prepare_smem(const void* kernel, int smem) {
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess)
+      return fail(VF_ERR_CUDA, "cudaFuncSetAttribute(smem=%d): %s", smem, cudaGetErrorString(e));
+  }
+  return VF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vf_version(void) { return 1; }
+
+const char* vf_last_error_string(void) { return g_err; }
+
+int vf_device_info(int* sm, int* major, int* minor) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(VF_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (sm) cudaDeviceGetAttribute(sm, cudaDevAttrMultiProcessorCount, dev);
+  if (major) cudaDeviceGetAttribute(major, cudaDevAttrComputeCapabilityMajor, dev);
+  if (minor) cudaDeviceGetAttribute(minor, cudaDevAttrComputeCapabilityMinor, dev);
+  return VF_OK;
+}
+
+int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, int* rows) {
+  if (!rows) return fail(VF_ERR_ARG, "vf_sample_rows: rows is NULL");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM)
+    return fail(VF_ERR_UNSUPPORTED, "vf_sample_rows: n_dim=%d outside [1, %d]", n_dim, VF_MAX_DIM);
+  if (precision != VF_PREC_F64 && precision != VF_PREC_F32)
+    return fail(VF_ERR_ARG, "vf_sample_rows: precision=%d", precision);
+  const void* k = sample_kernel(precision, n_dim, builtin_integrand(integrand) ? integrand : VF_INT_SYMGAUSS);
+  if (!k) return fail(VF_ERR_UNSUPPORTED, "vf_sample_rows: no kernel for integrand %d", integrand);
+  const int real = precision == VF_PREC_F64 ? 8 : 4;
+  const int smem = vf::sample_smem_bytes(real, n_dim, hist_copies_for(precision), train && alg == VF_ALG_VEGAS);
+  int rc = prepare_smem(k, smem);
+  if (rc) return rc;
+  int per_sm = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, VF_THREADS, smem);
+  if (e != cudaSuccess) return fail(VF_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  const int sms = sm_count();
+  if (sms <= 0) return fail(VF_ERR_CUDA, "no CUDA device");
+  *rows = (per_sm > 0 ? per_sm : 1) * sms;
+  return VF_OK;
+}
+
+int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n_events,
+              long long ev_offset, double xjac, const double* xmin, const double* xdelta,
+              double xdeltajac, const double* u_inj, unsigned long long seed,
+              unsigned int call_ctr, int integrand, const double* params, int train,
+              int accumulate, double* partials, int rows, int* ind_out, void* x_out,
+              void* w_out, void* f_out, int* flags, void* stream) {
+  if (alg != VF_ALG_VEGAS && alg != VF_ALG_PLAIN) return fail(VF_ERR_ARG, "vf_sample: alg=%d", alg);
+  if (precision != VF_PREC_F64 && precision != VF_PREC_F32)
+    return fail(VF_ERR_ARG, "vf_sample: precision=%d", precision);
+  if (n_dim < 1 || n_dim > VF_MAX_DIM)
+    return fail(VF_ERR_UNSUPPORTED, "vf_sample: n_dim=%d outside [1, %d]", n_dim, VF_MAX_DIM);
+  if (n_events < 0 || ev_offset < 0) return fail(VF_ERR_ARG, "vf_sample: negative event count/offset");
+  if (alg == VF_ALG_VEGAS && !grid) return fail(VF_ERR_ARG, "vf_sample: grid is NULL");
+  if ((xmin == nullptr) != (xdelta == nullptr))
+    return fail(VF_ERR_ARG, "vf_sample: xmin and xdelta must both be given or both NULL");
+  if (!builtin_integrand(integrand)) return fail(VF_ERR_ARG, "vf_sample: unknown integrand %d", integrand);
+  if ((integrand == VF_INT_SYMGAUSS || integrand == VF_INT_GAUSS || integrand == VF_INT_BREIT_WIGNER) &&
+      !params)
+    return fail(VF_ERR_ARG, "vf_sample: integrand %d needs params", integrand);
+  if (integrand != VF_INT_NONE && (!partials || rows < 1))
+    return fail(VF_ERR_ARG, "vf_sample: partials/rows required when evaluating");
+  if (rows < 1) rows = 1;
+  const void* k = sample_kernel(precision, n_dim, integrand);
+  if (!k) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no kernel for this configuration");
+
+  vf::SampleArgs a;
+  a.grid = grid;
+  a.xmin = xmin;
+  a.xdelta = xdelta;
+  a.u_inj = u_inj;
+  a.params = params;
+  a.partials = partials;
+  a.ind_out = ind_out;
+  a.x_out = x_out;
+  a.w_out = w_out;
+  a.f_out = f_out;
+  a.flags = flags;
+  a.n_events = n_events;
+  a.ev_offset = ev_offset;
+  a.xjac = xjac;
+  a.xdeltajac = xmin ? xdeltajac : 1.0;
+  a.seed = seed;
+  a.call_ctr = call_ctr;
+  a.n_dim = n_dim;
+  a.alg = alg;
+  a.train = train ? 1 : 0;
+  a.accumulate = accumulate ? 1 : 0;
+  a.hist_copies = hist_copies_for(precision);
+  const int real = precision == VF_PREC_F64 ? 8 : 4;
+  const int smem = vf::sample_smem_bytes(real, n_dim, a.hist_copies, a.train && alg == VF_ALG_VEGAS);
+  int rc = prepare_smem(k, smem);
+  if (rc) return rc;
+  void* args[] = {&a};
+  const cudaError_t e =
+      cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "vf_sample launch: %s", cudaGetErrorString(e));
+  return check_launch("vf_sample");
+}
+
+int vf_reduce_events(int precision, const void* f, const void* w, const int* ind,
+                     long long n_events, int n_dim, int n_out, int main_dim, int train,
+                     int accumulate, double* partials, int rows, int* flags, void* stream) {
+  if (!f || !w || !partials || rows < 1) return fail(VF_ERR_ARG, "vf_reduce_events: NULL buffer");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return fail(VF_ERR_UNSUPPORTED, "vf_reduce_events: n_dim=%d", n_dim);
+  if (n_out < 1 || main_dim < 0 || main_dim >= n_out)
+    return fail(VF_ERR_ARG, "vf_reduce_events: n_out=%d main_dim=%d", n_out, main_dim);
+  if (train && !ind) return fail(VF_ERR_ARG, "vf_reduce_events: ind required when train");
+  if (n_events < 0) return fail(VF_ERR_ARG, "vf_reduce_events: negative n_events");
+  vf::ReduceArgs a;
+  a.f = f;
+  a.w = w;
+  a.ind = ind;
+  a.partials = partials;
+  a.flags = flags;
+  a.n_events = n_events;
+  a.n_dim = n_dim;
+  a.n_out = n_out;
+  a.main_dim = main_dim;
+  a.train = train ? 1 : 0;
+  a.accumulate = accumulate ? 1 : 0;
+  const int smem = (n_dim * VF_BINS + 16) * (int)sizeof(double);
+  if (precision == VF_PREC_F64)
+    vf::vf_reduce_events_kernel<double><<<rows, 256, smem, (cudaStream_t)stream>>>(a);
+  else if (precision == VF_PREC_F32)
+    vf::vf_reduce_events_kernel<float><<<rows, 256, smem, (cudaStream_t)stream>>>(a);
+  else
+    return fail(VF_ERR_ARG, "vf_reduce_events: precision=%d", precision);
+  return check_launch("vf_reduce_events");
+}
+
+int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int train,
+                     double n_events, double alpha, double* grid, double* hist_out,
+                     double* sums_out, double* history, double* avg, int iter, int* flags,
+                     void* stream) {
+  if (!partials || rows < 1 || !history || !avg || iter < 0)
+    return fail(VF_ERR_ARG, "vf_iteration_end: NULL buffer or bad rows/iter");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return fail(VF_ERR_UNSUPPORTED, "vf_iteration_end: n_dim=%d", n_dim);
+  if (n_out < 1) return fail(VF_ERR_ARG, "vf_iteration_end: n_out=%d", n_out);
+  if (train && !grid) return fail(VF_ERR_ARG, "vf_iteration_end: grid required when train");
+  vf::IterEndArgs a;
+  a.partials = partials;
+  a.grid = grid;
+  a.hist_out = hist_out;
+  a.sums_out = sums_out;
+  a.history = history;
+  a.avg = avg;
+  a.flags = flags;
+  a.n_events = n_events;
+  a.alpha = alpha;
+  a.rows = rows;
+  a.n_dim = n_dim;
+  a.n_out = n_out;
+  a.train = train ? 1 : 0;
+  a.iter = iter;
+  const int blocks = (a.train || hist_out) ? n_dim + 1 : 1;
+  vf::vf_iteration_end_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(a);
+  return check_launch("vf_iteration_end");
+}
+
+int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, int* flags,
+                   void* stream) {
+  if (!grid || !hist) return fail(VF_ERR_ARG, "vf_refine_grid: NULL buffer");
+  if (n_dim < 1 || n_dim > 4096) return fail(VF_ERR_ARG, "vf_refine_grid: n_dim=%d", n_dim);
+  vf::vf_refine_kernel<<<n_dim, 64, 0, (cudaStream_t)stream>>>(grid, hist, alpha, flags);
+  return check_launch("vf_refine_grid");
+}
+
+int vf_consume_array_into_indices(const double* input, const int* indices, long long n,
+                                  int result_size, double* out, int* flags, void* stream) {
+  if (!out || result_size < 1) return fail(VF_ERR_ARG, "vf_consume_array_into_indices: bad output");
+  if (n > 0 && (!input || !indices)) return fail(VF_ERR_ARG, "vf_consume_array_into_indices: NULL input");
+  if (result_size > 12288) return fail(VF_ERR_UNSUPPORTED, "result_size %d > 12288", result_size);
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * result_size, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(VF_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+  if (n == 0) return VF_OK;
+  const int smem = result_size * (int)sizeof(double);
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(vf::vf_consume_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return fail(VF_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
+  }
+  long long blocks = (n + 255) / 256;
+  const int cap = 4 * (sm_count() > 0 ? sm_count() : 1);
+  if (blocks > cap) blocks = cap;
+  vf::vf_consume_kernel<<<(int)blocks, 256, smem, (cudaStream_t)stream>>>(input, indices, n, result_size,
+                                                                           out, flags);
+  return check_launch("vf_consume_array_into_indices");
+}
+
+}  // extern "C"

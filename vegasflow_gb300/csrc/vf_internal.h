@@ -1,0 +1,17 @@
+// Host-side internal declarations shared by the translation units of
+// libvegasgb.so (not part of the public C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace vf {
+
+// Kernel pointers of the ahead-of-time sampler instantiations
+// (dmax in {4, 8, 16}; integrand a VF_INT_* id), or nullptr.
+const void* sample_kernel_f64(int dmax, int integrand);
+const void* sample_kernel_f32(int dmax, int integrand);
+const void* plus_kernel_f64(int dmax, int integrand);
+const void* plus_kernel_f32(int dmax, int integrand);
+
+inline int dim_bucket(int n_dim) { return n_dim <= 4 ? 4 : (n_dim <= 8 ? 8 : 16); }
+
+}  // namespace vf

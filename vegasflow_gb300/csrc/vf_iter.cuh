@@ -1,0 +1,282 @@
+// Iteration-end work: reduce the per-block partial rows in a fixed order,
+// sigma, the running 1/sigma^2-weighted average and chi^2, and the grid
+// refinement (one block per dimension).  Also the standalone refinement, the
+// per-bin histogram utility and the reduction for torch-evaluated integrands.
+#pragma once
+#include "vf_device.cuh"
+
+namespace vf {
+
+struct IterEndArgs {
+  const double* partials;  // [rows][W], W = 2 n_out + 50 D
+  double* grid;            // [D][51], refined in place when train
+  double* hist_out;        // nullable [D][50]: the iteration's arr_res2
+  double* sums_out;        // nullable [2 n_out]: res, res2
+  double* history;         // [iterations][2 n_out]: res[n_out], sigma[n_out]
+  double* avg;             // [n_out][5]: sum res/s^2, sum 1/s^2, mean, sigma, chi2/dof
+  int* flags;              // nullable
+  double n_events;         // events of the iteration (the reference's n_events)
+  double alpha;            // grid damping exponent
+  int rows;
+  int n_dim;
+  int n_out;
+  int train;
+  int iter;
+};
+
+// vflow.py:135-211 for one dimension, by one block.  `h` is the dimension's
+// 50-bin histogram in shared memory; `row` the dimension's 51 edges in global
+// memory (read, then overwritten).
+__device__ inline void refine_dimension(const double* h, double* row, double alpha, int* flags) {
+  __shared__ double sub[VF_EDGES];
+  __shared__ double sm[VF_BINS];
+  __shared__ double wei[VF_BINS];
+  __shared__ double sum_t;
+  const int t = threadIdx.x;
+  if (t < VF_EDGES) sub[t] = row[t];
+  if (t < VF_BINS) {
+    // res_padded[1:-1] + res_padded[2:] + res_padded[:-2], zero padding (:156-158)
+    const double left = t > 0 ? h[t - 1] : 0.0;
+    const double right = t < VF_BINS - 1 ? h[t + 1] : 0.0;
+    const double v = (h[t] + right) + left;
+    const double meaner = (t == 0 || t == VF_BINS - 1) ? 2.0 : 3.0;
+    sm[t] = fmax(v / meaner, 1e-30);  // :159
+  }
+  __syncthreads();
+  if (t == 0) {
+    double s = 0.0;
+    for (int i = 0; i < VF_BINS; ++i) s += sm[i];  // :162
+    sum_t = s;
+  }
+  __syncthreads();
+  if (t < VF_BINS) {
+    const double aux = (1.0 - sm[t] / sum_t) / (log(sum_t) - log(sm[t]));  // :163-164
+    wei[t] = pow(aux, alpha);                                               // :165
+  }
+  __syncthreads();
+  if (t == 0) {
+    double ave = 0.0;
+    for (int i = 0; i < VF_BINS; ++i) ave += wei[i];
+    ave = ave / VF_BINS;  // :166
+    // :195-208, the while-loop state carried over the 49 outer steps
+    double bin_weight = 0.0, cur = 0.0, prev = 0.0;
+    int n_bin = -1;
+    int overrun = 0;
+    row[0] = 0.0;
+    for (int k = 0; k < VF_BINS - 1; ++k) {
+      while (bin_weight < ave) {
+        if (n_bin + 1 >= VF_BINS) {
+          overrun = 1;
+          break;
+        }
+        n_bin += 1;
+        bin_weight += wei[n_bin];
+        prev = cur;
+        cur = sub[n_bin + 1];
+      }
+      bin_weight -= ave;
+      const double delta = (cur - prev) * bin_weight / wei[n_bin];
+      row[k + 1] = cur - delta;
+    }
+    row[VF_BINS] = 1.0;
+    if (overrun && flags) atomicOr(flags, VF_FLAG_REFINE_OVERRUN);
+  }
+  __syncthreads();
+}
+
+// Block d < D (when train or hist_out): histogram of dimension d, then refine
+// it when train.  The last block: res/res2, sigma, history, average.
+__global__ void __launch_bounds__(256) vf_iteration_end_kernel(const IterEndArgs a) {
+  const int t = threadIdx.x;
+  const int D = a.n_dim;
+  const int K = a.n_out;
+  const int W = 2 * K + VF_BINS * D;
+  __shared__ double part[4][64];
+  __shared__ double hsm[VF_BINS];
+  const bool per_dim = a.train || a.hist_out != nullptr;
+  if (per_dim && (int)blockIdx.x < D) {
+    const int d = blockIdx.x;
+    const int c = t & 63, r0 = t >> 6;  // 4 row lanes x 64 columns
+    double s = 0.0;
+    if (c < VF_BINS)
+      for (int r = r0; r < a.rows; r += 4) s += a.partials[(long long)r * W + 2 * K + d * VF_BINS + c];
+    part[r0][c] = s;
+    __syncthreads();
+    if (t < VF_BINS) {
+      const double v = ((part[0][t] + part[1][t]) + part[2][t]) + part[3][t];
+      hsm[t] = v;
+      if (a.hist_out) a.hist_out[d * VF_BINS + t] = v;
+    }
+    __syncthreads();
+    if (a.train) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
+    return;
+  }
+  // ---- the sums, one output at a time
+  __shared__ double red[2][256];
+  for (int j = 0; j < K; ++j) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int r = t; r < a.rows; r += blockDim.x) {
+      s1 += a.partials[(long long)r * W + j];
+      s2 += a.partials[(long long)r * W + K + j];
+    }
+    red[0][t] = s1;
+    red[1][t] = s2;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (t < o) {
+        red[0][t] += red[0][t + o];
+        red[1][t] += red[1][t + o];
+      }
+      __syncthreads();
+    }
+    if (t == 0) {
+      const double res = red[0][0], res2 = red[1][0];
+      const double N = a.n_events;
+      // vflow.py:437-438 (and plain.py:37-43, the same expression)
+      const double err_tmp2 = __ddiv_rn(__dsub_rn(__dmul_rn(N, res2), __dmul_rn(res, res)), __dsub_rn(N, 1.0));
+      const double sigma = sqrt(fmax(err_tmp2, 0.0));
+      if (a.sums_out) {
+        a.sums_out[j] = res;
+        a.sums_out[K + j] = res2;
+      }
+      double* hrow = a.history + (long long)a.iter * 2 * K;
+      hrow[j] = res;
+      hrow[K + j] = sigma;
+      // monte_carlo.py:712-732, accumulated iteration by iteration
+      double* av = a.avg + 5 * j;
+      const double wgt = 1.0 / __dmul_rn(sigma, sigma);
+      av[0] = __dadd_rn(av[0], __dmul_rn(res, wgt));
+      av[1] = __dadd_rn(av[1], wgt);
+      const double mean = av[0] / av[1];
+      av[2] = mean;
+      av[3] = sqrt(1.0 / av[1]);
+      double chi2 = 0.0;
+      for (int i = 0; i <= a.iter; ++i) {
+        const double r = a.history[(long long)i * 2 * K + j];
+        const double sg = a.history[(long long)i * 2 * K + K + j];
+        chi2 += (r - mean) * (r - mean) / (sg * sg);
+      }
+      av[4] = a.iter > 0 ? chi2 / a.iter : 0.0;
+      if (!isfinite(res) || !isfinite(res2)) {
+        if (a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The reference's refine_grid(arr_res2): one block per dimension.
+__global__ void __launch_bounds__(64) vf_refine_kernel(double* grid, const double* hist, double alpha,
+                                                        int* flags) {
+  __shared__ double hsm[VF_BINS];
+  const int d = blockIdx.x;
+  if (threadIdx.x < VF_BINS) hsm[threadIdx.x] = hist[d * VF_BINS + threadIdx.x];
+  __syncthreads();
+  refine_dimension(hsm, grid + d * VF_EDGES, alpha, flags);
+}
+
+// utils.py:17-44: out[b] = sum of input[e] with indices[e] == b.  `out` must be
+// zeroed.  Shared-memory bins, then one float64 atomic per bin per block.
+__global__ void __launch_bounds__(256) vf_consume_kernel(const double* __restrict__ in,
+                                                         const int* __restrict__ idx, long long n,
+                                                         int size, double* out, int* flags) {
+  extern __shared__ double bins[];
+  for (int k = threadIdx.x; k < size; k += blockDim.x) bins[k] = 0.0;
+  __syncthreads();
+  int bad = 0;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int b = idx[e];
+    if (b < 0 || b >= size) {
+      bad = 1;
+      continue;
+    }
+    atomicAdd(&bins[b], in[e]);
+  }
+  if (bad && flags) atomicOr(flags, VF_FLAG_INDEX_RANGE);
+  __syncthreads();
+  for (int k = threadIdx.x; k < size; k += blockDim.x)
+    if (bins[k] != 0.0) atomicAdd(&out[k], bins[k]);
+}
+
+// Partial rows from integrand values computed outside the sampler (torch
+// callables): tmp = w f, tmp2 = tmp^2 per output; histogram of the main output.
+struct ReduceArgs {
+  const void* f;       // [n][n_out] (Real)
+  const void* w;       // [n] (Real), the full weight
+  const int* ind;      // [n][D]
+  double* partials;    // [rows][W], W = 2 n_out + 50 D
+  int* flags;
+  long long n_events;
+  int n_dim;
+  int n_out;
+  int main_dim;
+  int train;
+  int accumulate;
+};
+
+template <typename Real>
+__global__ void __launch_bounds__(256) vf_reduce_events_kernel(const ReduceArgs a) {
+  extern __shared__ double rsm[];  // [D*50] histogram, then [2][8][n_out] sums
+  const int D = a.n_dim, K = a.n_out;
+  const int nb = D * VF_BINS;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  double* hist = rsm;
+  double* wred = rsm + nb;
+  if (a.train)
+    for (int k = t; k < nb; k += blockDim.x) hist[k] = 0.0;
+  __syncthreads();
+  const Real* f = reinterpret_cast<const Real*>(a.f);
+  const Real* w = reinterpret_cast<const Real*>(a.w);
+  double* row = a.partials + (long long)blockIdx.x * (2 * K + nb);
+  for (int j = 0; j < K; ++j) {
+    double s1 = 0.0, s2 = 0.0;
+    for (long long e = (long long)blockIdx.x * blockDim.x + t; e < a.n_events;
+         e += (long long)gridDim.x * blockDim.x) {
+      // vflow.py:414-417: tmp = xjac * f (xjac reshaped to a column for vectorial f)
+      const double tmp = (double)w[e] * (double)f[e * K + j];
+      const double tmp2 = tmp * tmp;
+      s1 += tmp;
+      s2 += tmp2;
+      if (a.train && j == a.main_dim)
+        for (int d = 0; d < D; ++d) {
+          const int b = a.ind[e * D + d];
+          if (b >= 0 && b < VF_BINS) atomicAdd(&hist[d * VF_BINS + b], tmp2);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) {
+      wred[warp] = s1;
+      wred[8 + warp] = s2;
+    }
+    __syncthreads();
+    if (t == 0) {
+      double b1 = 0.0, b2 = 0.0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+        b1 += wred[i];
+        b2 += wred[8 + i];
+      }
+      if (a.accumulate) {
+        row[j] += b1;
+        row[K + j] += b2;
+      } else {
+        row[j] = b1;
+        row[K + j] = b2;
+      }
+    }
+    __syncthreads();
+  }
+  if (a.train)
+    for (int k = t; k < nb; k += blockDim.x) {
+      if (a.accumulate)
+        row[2 * K + k] += hist[k];
+      else
+        row[2 * K + k] = hist[k];
+    }
+}
+
+}  // namespace vf

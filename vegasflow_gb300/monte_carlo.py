@@ -1,0 +1,573 @@
+"""The Monte Carlo driver: ``MonteCarloFlow`` (vegasflow monte_carlo.py:95-741).
+
+Same public surface as the reference: ``MonteCarloFlow(n_dim, n_events,
+events_limit, list_devices, verbose, xmin, xmax)``, ``compile(integrand,
+compilable, signature, trace, check)``, ``run_integration(n_iter, log_time,
+histograms)``, ``run_event``, ``generate_random_array``, ``set_seed``, the
+``n_events`` / ``events_per_run`` / ``history`` / ``xjac`` properties, and the
+``wrapper`` / ``sampler`` helpers.  Extra keyword arguments: ``precision``
+("fp64" = the reference's float64 arithmetic, "fp32" = the fused fp32 form),
+``device`` and ``seed``.
+
+Execution model (one GPU):
+  * an integrand built with ``vegasflow_gb300.integrands`` runs *inside* the
+    sampler kernel: one launch per iteration samples, maps, evaluates and
+    reduces every event (``events_limit`` needs no chunking: the kernel keeps no
+    per-event state in memory);
+  * a torch callable runs on the sampler's x in HBM, chunk by chunk
+    (``events_per_run`` events per chunk, as the reference), followed by a
+    reduction kernel;
+  * per iteration one iteration-end kernel sums the block partials, computes
+    sigma, the running weighted average and chi^2, and refines the grid.  No
+    host synchronisation happens until ``run_integration`` returns (or each
+    iteration when ``verbose`` prints it).
+"""
+
+from __future__ import annotations
+
+import copy
+import inspect
+import logging
+import os
+import time
+from abc import ABC, abstractmethod
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .configflow import (
+    ALPHA,
+    BINS_MAX,
+    DEFAULT_ACTIVE_DEVICES,
+    DEFAULT_PRECISION,
+    DTYPE,
+    MAX_EVENTS_LIMIT,
+)
+from .integrands import DeviceIntegrand
+
+logger = logging.getLogger("vegasflow.monte_carlo")
+
+VF_MAX_DIM = 16
+
+
+def print_iteration(it, res, error, extra="", threshold=0.1):
+    """monte_carlo.py:61-69."""
+    if res < threshold:
+        return f"Result for iteration {it}: {res:.3e} +/- {error:.3e}" + extra
+    return f"Result for iteration {it}: {res:.4f} +/- {error:.4f}" + extra
+
+
+def _chunk_sizes(n_events, events_per_run):
+    """monte_carlo.py:437-452."""
+    out = []
+    left = int(n_events)
+    while left > 0:
+        out.append(min(left, events_per_run))
+        left -= events_per_run
+    return out
+
+
+def _random_seed():
+    return int.from_bytes(os.urandom(8), "little") & ((1 << 63) - 1)
+
+
+class MonteCarloFlow(ABC):
+    """Parent class of the integrators (monte_carlo.py:95)."""
+
+    _CAN_RUN_VECTORIAL = False
+    _ALG = nat.VF_ALG_PLAIN
+
+    def __init__(self, n_dim, n_events, events_limit=MAX_EVENTS_LIMIT,
+                 list_devices=DEFAULT_ACTIVE_DEVICES, verbose=True, xmin=None, xmax=None,
+                 precision=None, device=None, seed=None, **kwargs):
+        if "simplify_signature" in kwargs:
+            logger.warning("simplify_signature is deprecated and will be removed")
+        self.n_dim = int(n_dim)
+        if not 1 <= self.n_dim <= VF_MAX_DIM:
+            raise ValueError(f"n_dim={n_dim}: the GB300 sampler supports 1 to {VF_MAX_DIM} dimensions")
+        self._integrand = None
+        self._tf_integrand = None
+        self.event = None
+        self._verbose = verbose
+        self._history = []
+        self._n_events = int(n_events)
+        self._events_limit = int(events_limit)
+        self._events_per_run = min(self._events_limit, self._n_events)
+        self._compilation_arguments = None
+        self._vectorial = False
+        self._n_out = 1
+        self.distribute = False
+        self._pass_weight = False
+        self.list_devices = list_devices
+        self.devices = None
+        self.precision = (precision or DEFAULT_PRECISION).lower()
+        if self.precision not in ("fp64", "fp32"):
+            raise ValueError(f"precision must be 'fp64' or 'fp32', not {precision!r}")
+        self._prec = nat.VF_PREC_F64 if self.precision == "fp64" else nat.VF_PREC_F32
+        self._rdtype = torch.float64 if self.precision == "fp64" else torch.float32
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() \
+                else torch.device("cpu")
+        self.device = torch.device(device)
+        self._seed = _random_seed() if seed is None else int(seed)
+        self._call_ctr = 0
+        self._uniform_source = None
+        self._kind = None
+        self._rows = 0
+        self._ws = {}
+        self._it = 0
+
+        if xmin is not None or xmax is not None:  # monte_carlo.py:159-175
+            if xmin is None or xmax is None:
+                raise ValueError(
+                    "Both xmin and xmax must be provided if the integration limits are to change")
+            if not (len(xmin) == len(xmax) == n_dim):
+                raise ValueError("The integration limits must be given for all dimensions")
+            self._xmin_np = np.asarray(xmin, dtype=np.float64)
+            self._xdelta_np = np.asarray(xmax, dtype=np.float64) - self._xmin_np
+            if any(self._xdelta_np < 0.0):
+                raise ValueError(f"No xmin ({xmin}) can be bigger than xmax ({xmax})")
+            jac = self._xdelta_np[0]
+            for d in range(1, self.n_dim):
+                jac = jac * self._xdelta_np[d]
+            self._xdeltajac = float(jac)
+            self._xmin = torch.as_tensor(self._xmin_np, device=self.device)
+            self._xdelta = torch.as_tensor(self._xdelta_np, device=self.device)
+        else:
+            self._xmin = self._xdelta = None
+            self._xmin_np = self._xdelta_np = None
+            self._xdeltajac = None
+
+    # ---------------------------------------------------------------- properties
+    @property
+    def n_events(self):
+        """Number of events to run in a single iteration."""
+        return self._n_events
+
+    @n_events.setter
+    def n_events(self, val):
+        self._n_events = int(val)
+        self.events_per_run = self._events_limit
+        self._recompile()
+
+    @property
+    def events_per_run(self):
+        """Events per step of a torch-callable integrand (memory knob)."""
+        return self._events_per_run
+
+    @events_per_run.setter
+    def events_per_run(self, val):
+        self._events_per_run = min(int(val), self.n_events)
+        if self._events_per_run and self.n_events % self._events_per_run != 0:
+            logger.warning(
+                f"The number of events per run step {self._events_per_run} doesn't perfectly"
+                f"divide the number of events {self.n_events}, which can harm performance")
+
+    @property
+    def history(self):
+        """List of (result, error, histograms) per iteration."""
+        return self._history
+
+    @property
+    def xjac(self):
+        """The default Jacobian is 1 / total number of events."""
+        return 1.0 / self.n_events
+
+    # ---------------------------------------------------------------- seeds / rng
+    def set_seed(self, seed):
+        """Seed the Philox stream (key = seed; the per-iteration counter restarts)."""
+        self._seed = int(seed)
+        self._call_ctr = 0
+
+    def _next_call(self):
+        c = self._call_ctr
+        self._call_ctr += 1
+        return c & 0xFFFFFFFF
+
+    def set_uniform_source(self, source):
+        """Inject uniforms: ``source(n, n_dim)`` returns an (n, n_dim) float64 device
+        tensor of post-affine uniforms (U[TECH_CUT, 1-TECH_CUT)) used instead of the
+        in-kernel Philox stream for the next chunks; ``None`` restores Philox."""
+        self._uniform_source = source
+
+    # ---------------------------------------------------------------- abstract hooks
+    @abstractmethod
+    def _run_iteration(self):
+        """Run one iteration (``self.n_events``) of the integration."""
+
+    @abstractmethod
+    def _run_event(self, integrand, ncalls=None):
+        """Run one chunk of events; returns the accumulables."""
+
+    def _digest_random_generation(self, xrand, *args):
+        return xrand, 1.0
+
+    def _can_run_vectorial(self, expected_shape=None):
+        return self._CAN_RUN_VECTORIAL
+
+    def _grid_ptr(self):
+        return None
+
+    def _train_now(self):
+        return False
+
+    # ---------------------------------------------------------------- device helpers
+    def _require_gpu(self):
+        if self.device.type != "cuda":
+            raise RuntimeError("vegasflow_gb300 runs on a CUDA device only (no CPU fallback); "
+                               f"this integrator was created on {self.device}")
+        nat.load()
+
+    def _limits_ptrs(self):
+        if self._xmin is None:
+            return None, None, 1.0
+        return nat.ptr(self._xmin), nat.ptr(self._xdelta), self._xdeltajac
+
+    def _width(self):
+        return 2 * self._n_out + BINS_MAX * self.n_dim
+
+    def _workspace(self):
+        ws = self._ws
+        if ws.get("key") != (self._rows, self._width()):
+            ws.clear()
+            ws["key"] = (self._rows, self._width())
+            ws["partials"] = torch.zeros(self._rows * self._width(), dtype=torch.float64,
+                                         device=self.device)
+            ws["flags"] = torch.zeros(1, dtype=torch.int32, device=self.device)
+            ws["history"] = torch.zeros((16, 2 * self._n_out), dtype=torch.float64, device=self.device)
+            ws["avg"] = torch.zeros(5 * self._n_out, dtype=torch.float64, device=self.device)
+            ws["hist"] = torch.zeros((self.n_dim, BINS_MAX), dtype=torch.float64, device=self.device)
+            ws["sums"] = torch.zeros(2 * self._n_out, dtype=torch.float64, device=self.device)
+        return ws
+
+    def _history_slot(self):
+        ws = self._workspace()
+        if self._it >= ws["history"].shape[0]:
+            grow = torch.zeros((2 * ws["history"].shape[0], 2 * self._n_out), dtype=torch.float64,
+                               device=self.device)
+            grow[: ws["history"].shape[0]] = ws["history"]
+            ws["history"] = grow
+        return ws
+
+    def _reset_average(self):
+        ws = self._workspace()
+        ws["avg"].zero_()
+        self._it = 0
+
+    # ---------------------------------------------------------------- sampling
+    def _sample(self, n_events, ev_offset, call, integrand_id, params, train, accumulate,
+                u_inj=None, ind=None, x=None, w=None, f=None):
+        ws = self._workspace()
+        xmin, xdelta, xdj = self._limits_ptrs()
+        nat.call("vf_sample", self._ALG, self._prec, self._grid_ptr(), self.n_dim, int(n_events),
+                 int(ev_offset), float(self.xjac), xmin, xdelta, float(xdj), nat.ptr(u_inj),
+                 self._seed, call, int(integrand_id), nat.ptr(params), int(bool(train)),
+                 int(bool(accumulate)), nat.ptr(ws["partials"]), self._rows, nat.ptr(ind),
+                 nat.ptr(x), nat.ptr(w), nat.ptr(f), nat.ptr(ws["flags"]), nat.stream_handle())
+
+    def _injected(self, n):
+        if self._uniform_source is None:
+            return None
+        u = self._uniform_source(n, self.n_dim)
+        u = torch.as_tensor(u, dtype=torch.float64, device=self.device).contiguous()
+        if tuple(u.shape) != (n, self.n_dim):
+            raise ValueError(f"uniform source returned shape {tuple(u.shape)}, expected {(n, self.n_dim)}")
+        return u
+
+    def _fill_partials(self, train):
+        """All events of one iteration into the block-partial rows."""
+        self._require_gpu()
+        if self.event is None:
+            raise RuntimeError("Compile must be ran before running any iterations")
+        call = self._next_call()
+        if self._kind == "device":
+            n = self.n_events
+            if self._uniform_source is None:
+                self._sample(n, 0, call, self._int_id, self._params_dev, train, False)
+            else:
+                off = 0
+                for i, nc in enumerate(_chunk_sizes(n, self.events_per_run)):
+                    self._sample(nc, off, call, self._int_id, self._params_dev, train, i > 0,
+                                 u_inj=self._injected(nc))
+                    off += nc
+        else:
+            off = 0
+            for i, nc in enumerate(_chunk_sizes(self.n_events, self.events_per_run)):
+                self._torch_chunk(nc, off, call, train, accumulate=i > 0)
+                off += nc
+
+    def _chunk_buffers(self, nc):
+        ws = self._workspace()
+        cap = ws.get("xbuf").shape[0] if "xbuf" in ws else 0
+        if cap < nc:
+            ws["xbuf"] = torch.empty((nc, self.n_dim), dtype=self._rdtype, device=self.device)
+            ws["wbuf"] = torch.empty(nc, dtype=self._rdtype, device=self.device)
+            ws["ibuf"] = torch.empty((nc, self.n_dim), dtype=torch.int32, device=self.device)
+        return ws["xbuf"][:nc], ws["wbuf"][:nc], ws["ibuf"][:nc]
+
+    def _torch_chunk(self, nc, ev_offset, call, train, accumulate):
+        """Unfused path: sampler writes x, w, ind; torch evaluates; a kernel reduces."""
+        x, w, ind = self._chunk_buffers(nc)
+        self._sample(nc, ev_offset, call, nat.VF_INT_NONE, None, False, False,
+                     u_inj=self._injected(nc), ind=ind if self._ALG == nat.VF_ALG_VEGAS else None,
+                     x=x, w=w)
+        f = self._tf_integrand(x, weight=w)
+        f = torch.as_tensor(f).to(device=self.device, dtype=self._rdtype).reshape(nc, -1).contiguous()
+        ws = self._workspace()
+        nat.call("vf_reduce_events", self._prec, nat.ptr(f), nat.ptr(w),
+                 nat.ptr(ind) if self._ALG == nat.VF_ALG_VEGAS else None, int(nc), self.n_dim,
+                 self._n_out, int(getattr(self, "_main_dimension", 0)), int(bool(train)),
+                 int(bool(accumulate)), nat.ptr(ws["partials"]), self._rows, nat.ptr(ws["flags"]),
+                 nat.stream_handle())
+
+    def _end_iteration(self, train, n_events=None, want_hist=False, want_sums=False):
+        """Iteration-end kernel; returns (res, sigma) device views of the history row."""
+        ws = self._history_slot()
+        n = float(self.n_events if n_events is None else n_events)
+        nat.call("vf_iteration_end", nat.ptr(ws["partials"]), self._rows, self.n_dim, self._n_out,
+                 int(bool(train)), n, float(ALPHA), self._grid_ptr(),
+                 nat.ptr(ws["hist"]) if want_hist else None, nat.ptr(ws["sums"]) if want_sums else None,
+                 nat.ptr(ws["history"]), nat.ptr(ws["avg"]), int(self._it), nat.ptr(ws["flags"]),
+                 nat.stream_handle())
+        row = ws["history"][self._it]
+        self._it += 1
+        k = self._n_out
+        if self._vectorial:
+            return row[:k], row[k:]
+        return row[0], row[1]
+
+    def run_event(self, tensorize_events=False, **kwargs):
+        """Run all events of one iteration; returns the accumulated (res, res2[,
+        arr_res2]) as device tensors (monte_carlo.py:420-480)."""
+        want_hist = self._ALG == nat.VF_ALG_VEGAS and self._train_now()
+        self._fill_partials(train=want_hist)
+        ws = self._history_slot()
+        saved = self._it
+        # a scratch history slot so the running average is left untouched
+        nat.call("vf_iteration_end", nat.ptr(ws["partials"]), self._rows, self.n_dim, self._n_out, 0,
+                 float(self.n_events), float(ALPHA), self._grid_ptr(),
+                 nat.ptr(ws["hist"]) if want_hist else None, nat.ptr(ws["sums"]),
+                 nat.ptr(ws["history"]), nat.ptr(torch.zeros_like(ws["avg"])), int(saved),
+                 nat.ptr(ws["flags"]), nat.stream_handle())
+        k = self._n_out
+        res = ws["sums"][:k].clone()
+        res2 = ws["sums"][k:].clone()
+        if not self._vectorial:
+            res, res2 = res[0], res2[0]
+        if want_hist:
+            return res, res2, ws["hist"].clone()
+        return res, res2
+
+    # ---------------------------------------------------------------- random numbers
+    def generate_random_array(self, n_events, *args):
+        """(x, p(x)) for ``n_events`` points (monte_carlo.py:229-247)."""
+        rnds, xjac_raw, *extra = self._generate_random_array(n_events, *args)
+        xjac = xjac_raw / (self.xjac * n_events)
+        return rnds, xjac
+
+    def _generate_random_array(self, n_events, *args):
+        """(x, w[, ind]) of ``n_events`` points, weighted as part of an
+        ``self.n_events`` iteration (monte_carlo.py:249-275)."""
+        self._require_gpu()
+        n = int(n_events)
+        x = torch.empty((n, self.n_dim), dtype=self._rdtype, device=self.device)
+        w = torch.empty(n, dtype=self._rdtype, device=self.device)
+        ind = torch.empty((n, self.n_dim), dtype=torch.int32, device=self.device) \
+            if self._ALG == nat.VF_ALG_VEGAS else None
+        self._sample(n, 0, self._next_call(), nat.VF_INT_NONE, None, False, False,
+                     u_inj=self._injected(n), ind=ind, x=x, w=w)
+        if ind is None:
+            return x, w
+        return x, w, ind
+
+    # ---------------------------------------------------------------- compile
+    def trace(self, n_events=50):
+        rnds, wgt, *_ = self._generate_random_array(n_events)
+        if self._kind == "torch":
+            self._tf_integrand(rnds, weight=wgt)
+
+    def compile(self, integrand, compilable=True, signature=None, trace=False, check=True):
+        """Register the integrand (monte_carlo.py:489-636).
+
+        ``integrand`` is either a ``DeviceIntegrand`` (evaluated inside the
+        sampler kernel) or a callable on torch tensors ``f(xarr[, weight][,
+        n_dim])`` returning ``(n,)`` or, for VegasFlow/PlainFlow, ``(n, k)``.
+        ``compilable`` and ``signature`` are accepted for compatibility (there is
+        no tracing compiler); ``check`` runs the reference's 23-event shape check
+        on torch callables."""
+        kwargs = {"compilable": compilable, "signature": signature, "trace": trace}
+        self._compilation_arguments = (integrand, kwargs)
+        self._integrand = integrand
+        self._vectorial = False
+        self._n_out = 1
+        if isinstance(integrand, DeviceIntegrand):
+            integrand.check_dims(self.n_dim)
+            self._kind = "device"
+            self._int_id = integrand.integrand_id
+            self._params_host = integrand.params(self.n_dim)
+            self._params_dev = torch.as_tensor(self._params_host, dtype=torch.float64,
+                                               device=self.device) if self.device.type == "cuda" else None
+            self._tf_integrand = integrand
+        else:
+            if not callable(integrand):
+                raise TypeError("the integrand must be callable or a DeviceIntegrand")
+            self._kind = "torch"
+            try:
+                args = inspect.getfullargspec(integrand).args[1:]
+            except TypeError:
+                args = []
+            n_dim = self.n_dim
+
+            def new_integrand(xarr, weight=None, **kw):
+                if "weight" in args and "n_dim" in args:
+                    return integrand(xarr, n_dim=n_dim, weight=weight, **kw)
+                if "weight" in args:
+                    return integrand(xarr, weight=weight, **kw)
+                if "n_dim" in args:
+                    return integrand(xarr, n_dim=n_dim, **kw)
+                return integrand(xarr, **kw)
+
+            self._tf_integrand = new_integrand
+            if check:
+                event_size = 23
+                test_array = torch.rand((event_size, self.n_dim), dtype=self._rdtype, device=self.device)
+                wgt = torch.rand(event_size, dtype=self._rdtype, device=self.device)
+                res_tmp = torch.as_tensor(new_integrand(test_array, weight=wgt))
+                res_shape = tuple(res_tmp.shape)
+                expected_shape = (event_size,)
+                if len(res_shape) == 2:
+                    self._vectorial = True
+                    expected_shape = tuple(res_tmp.reshape(event_size, -1).shape)
+                    if not self._can_run_vectorial(expected_shape):
+                        raise NotImplementedError(
+                            f"The {self.__class__.__name__} algorithm does not support vectorial "
+                            "integrands")
+                    self._n_out = expected_shape[1]
+                if res_shape != expected_shape:
+                    error_str = "the shape of the integrand output should be: (n_events,"
+                    if self._vectorial:
+                        error_str += " output_dim,"
+                    logger.error(f"Wrong integrand output shape, {error_str})")
+                    raise ValueError(
+                        "The integrand is not returning a value per event, expected shape: "
+                        f"{expected_shape}, found: {res_shape}")
+        self.event = self._fill_partials
+        if self.device.type == "cuda":
+            self._choose_rows()
+            self._ws.clear()
+        if trace:
+            self.trace(n_events=23)
+
+    def _choose_rows(self):
+        lib = nat.load()
+        import ctypes
+        rows = ctypes.c_int(0)
+        integ = self._int_id if self._kind == "device" else nat.VF_INT_SYMGAUSS
+        nat.check(lib.vf_sample_rows(self._ALG, self._prec, self.n_dim, integ, 1, ctypes.byref(rows)))
+        self._rows = max(1, rows.value)
+
+    def _recompile(self):
+        if self._compilation_arguments is None:
+            raise RuntimeError("recompile was called without ever having called compile")
+        self.compile(self._compilation_arguments[0], **self._compilation_arguments[1])
+
+    # ---------------------------------------------------------------- integration
+    def run_integration(self, n_iter, log_time=True, histograms=None):
+        """Run ``n_iter`` iterations; returns (result, sigma) (monte_carlo.py:645-741)."""
+        self._require_gpu()
+        self._reset_average()
+        first = len(self._history)
+        all_results = []
+        for i in range(n_iter):
+            if log_time:
+                start = time.time()
+            res, error = self._run_iteration()
+            all_results.append((res, error))
+            hist_copy = copy.deepcopy(histograms) if histograms else None
+            if histograms:
+                for h in histograms:
+                    h.zero_()
+            self._history.append([res, error, hist_copy])
+            if self._verbose:
+                torch.cuda.current_stream().synchronize()
+                time_str = f"(took {time.time() - start:.5f} s)" if log_time else ""
+                if self._vectorial:
+                    info = [print_iteration(i, float(rr), float(ee), extra=f" [dimension {d}] {time_str}")
+                            for d, (rr, ee) in enumerate(zip(res.tolist(), error.tolist()))]
+                else:
+                    info = [print_iteration(i, float(res), float(error), extra=time_str)]
+                logger.info("\n      ".join(info))
+        ws = self._workspace()
+        host = torch.cat([ws["history"][: self._it].reshape(-1), ws["avg"],
+                          ws["flags"].to(torch.float64)]).cpu().numpy()
+        k = self._n_out
+        hist_rows = host[: self._it * 2 * k].reshape(self._it, 2 * k)
+        avg = host[self._it * 2 * k: self._it * 2 * k + 5 * k].reshape(k, 5)
+        flags = int(host[-1])
+        self._check_flags(flags)
+        base = self._it - n_iter
+        for i in range(n_iter):
+            r, s = hist_rows[base + i][:k], hist_rows[base + i][k:]
+            self._history[first + i][0] = r.copy() if self._vectorial else np.float64(r[0])
+            self._history[first + i][1] = s.copy() if self._vectorial else np.float64(s[0])
+            self._history[first + i] = tuple(self._history[first + i])
+        if histograms:
+            weight_sum = 0.0
+            for h in histograms:
+                h.zero_()
+            for i in range(n_iter):
+                wgt = 1.0 / np.power(self._history[first + i][1], 2)
+                weight_sum += wgt
+                for aux_h, curr_h in zip(histograms, self._history[first + i][2]):
+                    aux_h.add_(curr_h * float(np.mean(wgt)))
+            for h in histograms:
+                h.div_(float(np.mean(weight_sum)))
+        self.chi2_dof = avg[:, 4].copy() if self._vectorial else float(avg[0, 4])
+        if self._vectorial:
+            final_result, sigma = avg[:, 2].copy(), avg[:, 3].copy()
+            if self._verbose:
+                logger.info("\n     ".join(f"Final results [dim = {d}]: {rr:g} +/- {ee:g}"
+                                           for d, (rr, ee) in enumerate(zip(final_result, sigma))))
+        else:
+            final_result, sigma = np.float64(avg[0, 2]), np.float64(avg[0, 3])
+            if self._verbose:
+                logger.info(f" > Final results: {final_result:g} +/- {sigma:g}")
+        return final_result, sigma
+
+    def _check_flags(self, flags):
+        if flags & nat.VF_FLAG_INDEX_RANGE:
+            logger.warning("some uniforms mapped outside the grid and were clamped (injected "
+                           "uniforms outside [0, 1)?)")
+        if flags & nat.VF_FLAG_REFINE_OVERRUN:
+            logger.warning("grid refinement walked past the last bin (rounding); clamped")
+        if flags & nat.VF_FLAG_NONFINITE:
+            logger.warning("a partial sum was NaN or Inf")
+        if flags:
+            self._workspace()["flags"].zero_()
+
+    def make_differentiable(self):
+        raise NotImplementedError(
+            "make_differentiable: gradients through the GPU sampler are not provided; "
+            "integrate with a torch callable and differentiate its inputs instead")
+
+    def set_distribute(self, queue_object):
+        raise NotImplementedError("dask distribution is not part of the GB300 build (one GPU)")
+
+
+def wrapper(integrator_class, integrand, n_dim, n_iter, total_n_events, compilable=True, **kwargs):
+    """monte_carlo.py:744-762."""
+    mc_instance = integrator_class(n_dim, total_n_events, **kwargs)
+    mc_instance.compile(integrand, compilable=compilable)
+    return mc_instance.run_integration(n_iter)
+
+
+def sampler(integrator_class, integrand, n_dim, total_n_events, training_steps=5, compilable=True,
+            return_class=False, **kwargs):
+    """monte_carlo.py:765-794."""
+    mc_instance = integrator_class(n_dim, total_n_events, verbose=False, **kwargs)
+    mc_instance.compile(integrand, compilable=compilable)
+    _ = mc_instance.run_integration(training_steps, log_time=False)
+    if return_class:
+        return mc_instance
+    return mc_instance.generate_random_array
