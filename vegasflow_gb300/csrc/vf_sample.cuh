@@ -124,9 +124,11 @@ vf_sample_kernel(const SampleArgs a) {
   p += fill_hist ? a.hist_copies * nb * (int)sizeof(Real) : 0;
   Real* lim = reinterpret_cast<Real*>(p);  // [2][VF_MAX_DIM] xmin, xdelta
 
+  // the grid exists (and is read) only for the VEGAS map; plain MC passes NULL
   if constexpr (sizeof(Real) == 8) {
-    for (int k = tid; k < D * VF_EDGES; k += blockDim.x) edges[k] = a.grid[k];
-  } else {
+    if (vegas)
+      for (int k = tid; k < D * VF_EDGES; k += blockDim.x) edges[k] = a.grid[k];
+  } else if (vegas) {
     for (int k = tid; k < nb; k += blockDim.x) {
       const int d = k / VF_BINS, b = k - d * VF_BINS;
       const double lo = a.grid[d * VF_EDGES + b];
