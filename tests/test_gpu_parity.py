@@ -213,8 +213,16 @@ def test_c2_injected_1e7_bit_exact_indices_and_integral():
     assert np.array_equal(x.cpu().numpy(), ox)
     assert np.array_equal(w.cpu().numpy(), ow)
     del x, w, ind
-    inst.set_uniform_source(lambda m, d: ud)
+    pos = [0]
+
+    def chunks(m, d):  # consecutive rows, one events_limit chunk at a time
+        blk = ud[pos[0]:pos[0] + m]
+        pos[0] += m
+        return blk
+
+    inst.set_uniform_source(chunks)
     r, s = (float(v) for v in inst._run_iteration())
+    assert pos[0] == n
     orc = oracle.OracleVegas(n_dim, n)
     ref = orc.iteration(lambda m, d: u, symgauss_np)
     np.testing.assert_allclose([r, s], ref, rtol=1e-10)
