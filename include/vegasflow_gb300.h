@@ -54,6 +54,9 @@ extern "C" {
 #define VF_INT_SUM 5           /* none                                           */
 #define VF_INT_JIT_BASE 1000   /* ids returned by vf_jit_integrand               */
 
+/* ---- tunables (vf_tune_set / vf_tune_get) ---------------------------------- */
+#define VF_TUNE_F32_HIST_COPIES 1 /* histogram copies per warp, fp32 VEGAS sampler: 1|2|4 */
+
 int vf_version(void);
 const char* vf_last_error_string(void);
 /* SM count and compute capability of the current device. */
@@ -124,6 +127,13 @@ int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, in
 /* consume_array_into_indices (utils.py:17-44): out[size] = per-bin sums. */
 int vf_consume_array_into_indices(const double* input, const int* indices, long long n,
                                   int result_size, double* out, int* flags, void* stream);
+
+/*
+ * Process-wide tunables picked by the autotuner (no counterpart in the
+ * reference, whose kernels are TensorFlow's).  Values apply to later launches.
+ */
+int vf_tune_set(int key, int value);
+int vf_tune_get(int key, int* value);
 
 /*
  * Calibration (no counterpart in the reference): `blocks` x 256 threads each

@@ -28,6 +28,20 @@ def symgauss_np(x):
     return oracle.integrand_symgauss(x, 0.1)
 
 
+class chunked:
+    """Uniform source handing out consecutive rows of ``arr``, one events_limit
+    chunk per call (the order in which the iteration consumes them)."""
+
+    def __init__(self, arr):
+        self.arr = arr
+        self.pos = 0
+
+    def __call__(self, m, d):
+        blk = self.arr[self.pos:self.pos + m]
+        self.pos += m
+        return blk
+
+
 def test_map_bit_exact_against_reference(golden):
     """vflow.py:93-126 on the reference's own uniforms and trained grid."""
     grid = golden["map/grid"]
@@ -213,18 +227,12 @@ def test_c2_injected_1e7_bit_exact_indices_and_integral():
     assert np.array_equal(x.cpu().numpy(), ox)
     assert np.array_equal(w.cpu().numpy(), ow)
     del x, w, ind
-    pos = [0]
-
-    def chunks(m, d):  # consecutive rows, one events_limit chunk at a time
-        blk = ud[pos[0]:pos[0] + m]
-        pos[0] += m
-        return blk
-
-    inst.set_uniform_source(chunks)
+    gpu_src = chunked(ud)
+    inst.set_uniform_source(gpu_src)
     r, s = (float(v) for v in inst._run_iteration())
-    assert pos[0] == n
+    assert gpu_src.pos == n
     orc = oracle.OracleVegas(n_dim, n)
-    ref = orc.iteration(lambda m, d: u, symgauss_np)
+    ref = orc.iteration(chunked(u), symgauss_np)
     np.testing.assert_allclose([r, s], ref, rtol=1e-10)
     np.testing.assert_allclose(inst.divisions.cpu().numpy(), orc.divisions, rtol=0, atol=1e-12)
 

@@ -40,6 +40,8 @@ VF_INT_PROD = 4
 VF_INT_SUM = 5
 VF_INT_JIT_BASE = 1000
 
+VF_TUNE_F32_HIST_COPIES = 1
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _LL = ctypes.c_longlong
@@ -60,6 +62,8 @@ SIGNATURES = {
     "vf_refine_grid": [_P, _P, _I, _D, _P, _P],
     "vf_consume_array_into_indices": [_P, _P, _LL, _I, _P, _P, _P],
     "vf_issue_probe": [_P, _I, _I, _P, _P],
+    "vf_tune_set": [_I, _I],
+    "vf_tune_get": [_I, _P],
 }
 _RESTYPE = {"vf_last_error_string": ctypes.c_char_p}
 

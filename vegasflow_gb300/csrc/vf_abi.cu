@@ -1,5 +1,6 @@
 // The extern "C" entry points of libvegasgb.so (declared in
 // include/vegasflow_gb300.h): argument checks, kernel selection, launch.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -8,8 +9,12 @@
 #include "vf_internal.h"
 #include "vf_iter.cuh"
 #include "vf_sample.cuh"
+#include "vf_vegas_f32.cuh"
 
 namespace {
+
+// Tunables (vf_tune_set): histogram copies per warp of the fp32 VEGAS sampler.
+std::atomic<int> g_f32_hist_copies{2};
 
 thread_local char g_err[1024] = "";
 
@@ -46,6 +51,25 @@ const void* sample_kernel(int precision, int n_dim, int integrand) {
                                   : vf::sample_kernel_f32(dmax, integrand);
 }
 
+bool evaluating_builtin(int id) { return id >= VF_INT_SYMGAUSS && id <= VF_INT_SUM; }
+
+// The specialised fp32 VEGAS kernel serves evaluating launches without taps.
+bool use_vegas_f32(int alg, int precision, int integrand, bool taps) {
+  return precision == VF_PREC_F32 && alg == VF_ALG_VEGAS && evaluating_builtin(integrand) && !taps;
+}
+
+void fill_philox(vf::SampleArgs& a, unsigned long long seed, unsigned int call) {
+  unsigned int k0 = (unsigned int)seed, k1 = (unsigned int)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    a.rk.k0[r] = k0;
+    a.rk.k1[r] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  for (int q = 0; q < 4; ++q) a.ctr2[q] = (call << 4) | (unsigned int)q;
+  a.ctr3 = call >> 28;
+}
+
 int prepare_smem(const void* kernel, int smem) {
   if (smem > 48 * 1024) {
     const cudaError_t e =
@@ -61,6 +85,25 @@ int prepare_smem(const void* kernel, int smem) {
 extern "C" {
 
 int vf_version(void) { return 1; }
+
+int vf_tune_set(int key, int value) {
+  if (key == VF_TUNE_F32_HIST_COPIES) {
+    if (value != 1 && value != 2 && value != 4)
+      return fail(VF_ERR_ARG, "vf_tune_set: histogram copies per warp must be 1, 2 or 4");
+    g_f32_hist_copies.store(value);
+    return VF_OK;
+  }
+  return fail(VF_ERR_ARG, "vf_tune_set: unknown key %d", key);
+}
+
+int vf_tune_get(int key, int* value) {
+  if (!value) return fail(VF_ERR_ARG, "vf_tune_get: value is NULL");
+  if (key == VF_TUNE_F32_HIST_COPIES) {
+    *value = g_f32_hist_copies.load();
+    return VF_OK;
+  }
+  return fail(VF_ERR_ARG, "vf_tune_get: unknown key %d", key);
+}
 
 const char* vf_last_error_string(void) { return g_err; }
 
@@ -80,10 +123,18 @@ int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, 
     return fail(VF_ERR_UNSUPPORTED, "vf_sample_rows: n_dim=%d outside [1, %d]", n_dim, VF_MAX_DIM);
   if (precision != VF_PREC_F64 && precision != VF_PREC_F32)
     return fail(VF_ERR_ARG, "vf_sample_rows: precision=%d", precision);
-  const void* k = sample_kernel(precision, n_dim, builtin_integrand(integrand) ? integrand : VF_INT_SYMGAUSS);
+  const int integ = builtin_integrand(integrand) ? integrand : VF_INT_SYMGAUSS;
+  const void* k;
+  int smem;
+  if (use_vegas_f32(alg, precision, integ, false)) {
+    k = vf::vegas_f32_kernel(n_dim, integ);
+    smem = vf::vegas_f32_smem_bytes(n_dim, g_f32_hist_copies.load(), train);
+  } else {
+    k = sample_kernel(precision, n_dim, integ);
+    const int real = precision == VF_PREC_F64 ? 8 : 4;
+    smem = vf::sample_smem_bytes(real, n_dim, hist_copies_for(precision), train && alg == VF_ALG_VEGAS);
+  }
   if (!k) return fail(VF_ERR_UNSUPPORTED, "vf_sample_rows: no kernel for integrand %d", integrand);
-  const int real = precision == VF_PREC_F64 ? 8 : 4;
-  const int smem = vf::sample_smem_bytes(real, n_dim, hist_copies_for(precision), train && alg == VF_ALG_VEGAS);
   int rc = prepare_smem(k, smem);
   if (rc) return rc;
   int per_sm = 0;
@@ -117,7 +168,9 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   if (integrand != VF_INT_NONE && (!partials || rows < 1))
     return fail(VF_ERR_ARG, "vf_sample: partials/rows required when evaluating");
   if (rows < 1) rows = 1;
-  const void* k = sample_kernel(precision, n_dim, integrand);
+  const bool taps = ind_out || x_out || w_out || f_out;
+  const bool fast = use_vegas_f32(alg, precision, integrand, taps);
+  const void* k = fast ? vf::vegas_f32_kernel(n_dim, integrand) : sample_kernel(precision, n_dim, integrand);
   if (!k) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no kernel for this configuration");
 
   vf::SampleArgs a;
@@ -142,9 +195,16 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   a.alg = alg;
   a.train = train ? 1 : 0;
   a.accumulate = accumulate ? 1 : 0;
-  a.hist_copies = hist_copies_for(precision);
-  const int real = precision == VF_PREC_F64 ? 8 : 4;
-  const int smem = vf::sample_smem_bytes(real, n_dim, a.hist_copies, a.train && alg == VF_ALG_VEGAS);
+  fill_philox(a, seed, call_ctr);
+  int smem;
+  if (fast) {
+    a.hist_copies = g_f32_hist_copies.load();
+    smem = vf::vegas_f32_smem_bytes(n_dim, a.hist_copies, a.train);
+  } else {
+    a.hist_copies = hist_copies_for(precision);
+    const int real = precision == VF_PREC_F64 ? 8 : 4;
+    smem = vf::sample_smem_bytes(real, n_dim, a.hist_copies, a.train && alg == VF_ALG_VEGAS);
+  }
   int rc = prepare_smem(k, smem);
   if (rc) return rc;
   void* args[] = {&a};

@@ -58,6 +58,18 @@ __device__ __forceinline__ void philox4x32_10(u32& c0, u32& c1, u32& c2, u32& c3
   }
 }
 
+// Round keys precomputed on the host (k + r W for r = 0..9): passed in the
+// kernel's parameter block, they become constant-bank operands of the xors.
+struct RoundKeys {
+  u32 k0[10], k1[10];
+};
+
+__device__ __forceinline__ void philox4x32_10_rk(u32& c0, u32& c1, u32& c2, u32& c3,
+                                                 const RoundKeys& rk) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) philox_round(c0, c1, c2, c3, rk.k0[r], rk.k1[r]);
+}
+
 // The 4 words of block q of event ev for sampler call `call`.
 __device__ __forceinline__ void philox_block(u64 ev, u32 call, u32 q, Key key, u32 w[4]) {
   u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = (call << 4) | q, c3 = call >> 28;

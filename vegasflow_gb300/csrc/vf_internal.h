@@ -12,6 +12,14 @@ const void* sample_kernel_f32(int dmax, int integrand);
 const void* plus_kernel_f64(int dmax, int integrand);
 const void* plus_kernel_f32(int dmax, int integrand);
 
+// The fp32 VEGAS sampler specialised on the exact dimension count (1..8 in
+// part a, 9..16 in part b).
+const void* vegas_f32_kernel_a(int n_dim, int integrand);
+const void* vegas_f32_kernel_b(int n_dim, int integrand);
+inline const void* vegas_f32_kernel(int n_dim, int integrand) {
+  return n_dim <= 8 ? vegas_f32_kernel_a(n_dim, integrand) : vegas_f32_kernel_b(n_dim, integrand);
+}
+
 inline int dim_bucket(int n_dim) { return n_dim <= 4 ? 4 : (n_dim <= 8 ? 8 : 16); }
 
 }  // namespace vf

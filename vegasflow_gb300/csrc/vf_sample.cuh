@@ -44,8 +44,22 @@ struct SampleArgs {
   int alg;                  // 0 = VEGAS importance map, 1 = plain MC
   int train;                // fill the histogram
   int accumulate;           // 0: store rows, 1: add to rows
-  int hist_copies;          // 1: one block histogram, >1: per-warp copies
+  int hist_copies;          // generic kernel: 1 = one block histogram, >1 = per-warp copies;
+                            // fp32 VEGAS kernel: copies per warp (1, 2, 4)
+  RoundKeys rk;             // Philox round keys (seed + r W, r = 0..9), host-computed
+  unsigned int ctr2[4];     // Philox counter word 2 of 4-word block q: (call << 4) | q
+  unsigned int ctr3;        // Philox counter word 3: call >> 28
 };
+
+// The 4 words of block q of event ev, with the host-computed keys/counters.
+__device__ __forceinline__ void philox_words(u64 ev, const SampleArgs& a, int q, u32 w[4]) {
+  u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+  philox4x32_10_rk(c0, c1, c2, c3, a.rk);
+  w[0] = c0;
+  w[1] = c1;
+  w[2] = c2;
+  w[3] = c3;
+}
 
 template <typename Real>
 struct GridSmemBytes;
@@ -148,7 +162,6 @@ vf_sample_kernel(const SampleArgs a) {
   IntegrandConsts<Real, DMAX> kc;
   load_consts<DMAX>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
   Real* my_hist = hist + (warp % a.hist_copies) * nb;
-  const Key key = {(u32)a.seed, (u32)(a.seed >> 32)};
   const double xjac = a.xjac;
   const double xdeltajac = a.xdeltajac;
   // float64 factor of the fp32 form's weight: 50^D (VEGAS Jacobian constant) * xjac * prod(xdelta)
@@ -179,7 +192,7 @@ vf_sample_kernel(const SampleArgs a) {
         for (int q = 0; q < (DMAX + 1) / 2; ++q)
           if (2 * q < D) {
             u32 wd[4];
-            philox_block(ev, a.call_ctr, (u32)q, key, wd);
+            philox_words(ev, a, q, wd);
             u[2 * q] = tech_cut(u53(wd[0], wd[1]));
             if (2 * q + 1 < DMAX) u[2 * q + 1] = tech_cut(u53(wd[2], wd[3]));
           }
@@ -264,7 +277,7 @@ vf_sample_kernel(const SampleArgs a) {
         for (int q = 0; q < (DMAX + 3) / 4; ++q)
           if (4 * q < D) {
             u32 r[4];
-            philox_block(ev, a.call_ctr, (u32)q, key, r);
+            philox_words(ev, a, q, r);
 #pragma unroll
             for (int j = 0; j < 4; ++j)
               if (4 * q + j < DMAX) wd[4 * q + j] = r[j];

@@ -1,0 +1,221 @@
+// The fused fp32 VEGAS sampler: the performance path of the float32 form.
+//
+// Compared with the generic sampler (vf_sample.cuh) this kernel is specialised
+// at compile time on the exact dimension count and the integrand, draws the
+// Philox words with round keys held in the parameter block, and stages a
+// per-bin table that folds the importance map, the integration limits and --
+// for the Gaussian family -- the integrand's affine argument into one fused
+// multiply-add per dimension:
+//
+//   bin i, fraction m in [1, 2) from p = 50 * ~word + 25 (exact, 64-bit):
+//       i = p >> 32,  m = 1 + (p mod 2^32) / 2^32  (23 bits)
+//   table cell {c0, c1} per (dimension, bin), computed in float64 and rounded once:
+//       generic integrand:  x  = c0 + c1 m,  c0 = xmin + (lo - delta) xdelta, c1 = delta xdelta
+//       Gaussian family:    t  = c0 + c1 m,  t = (x - mu) sqrt(log2 e) / a,
+//                           f  = 2^(-sum t^2)  (the normalisation goes to the float64 scale)
+//   weight w = prod_d c1 (float32); the constant 50^D * xjac (* pref / prod k) is
+//   applied in float64 to the block partials.
+//
+// Per event: accumulation of w f and (w f)^2 in TwoSum-compensated fp32, and
+// (when training) the (w f)^2 histogram in shared memory with `hist_copies`
+// copies per warp (lanes split into groups to thin same-address collisions).
+#pragma once
+#include "vf_sample.cuh"
+
+#ifndef VF_F32_MIN_BLOCKS
+#define VF_F32_MIN_BLOCKS 4
+#endif
+
+namespace vf {
+
+__device__ __forceinline__ float ex2_approx_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, int train) {
+  return D * VF_BINS * 8 + (train ? (VF_THREADS / 32) * copies_per_warp * D * VF_BINS * 4 : 0);
+}
+
+template <int D, int INTEG>
+__global__ void __launch_bounds__(VF_THREADS, VF_F32_MIN_BLOCKS)
+vf_vegas_f32_kernel(const SampleArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NB = D * VF_BINS;
+  constexpr bool GAUSS = (INTEG == VF_INT_SYMGAUSS || INTEG == VF_INT_GAUSS);
+  constexpr double SQRT_LOG2E = 1.2011224087864498;  // sqrt(log2(e))
+  float2* cells = reinterpret_cast<float2*>(smem);
+  float* hist = reinterpret_cast<float*>(smem + NB * sizeof(float2));
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const bool train = a.train != 0;
+  const bool limits = a.xmin != nullptr;
+  const int cpw = a.hist_copies;
+
+  // ---- stage the per-bin table (float64, rounded once) and clear the histograms
+  for (int k = tid; k < NB; k += blockDim.x) {
+    const int d = k / VF_BINS, b = k - d * VF_BINS;
+    const double lo = a.grid[d * VF_EDGES + b];
+    const double dl = a.grid[d * VF_EDGES + b + 1] - lo;
+    double c0 = lo - dl, c1 = dl;
+    if (limits) {
+      c0 = a.xmin[d] + c0 * a.xdelta[d];
+      c1 = c1 * a.xdelta[d];
+    }
+    if (GAUSS) {
+      const double mu = (INTEG == VF_INT_SYMGAUSS) ? 0.5 : a.params[d];
+      const double kk = SQRT_LOG2E / ((INTEG == VF_INT_SYMGAUSS) ? a.params[0] : a.params[D + d]);
+      c0 = (c0 - mu) * kk;
+      c1 = c1 * kk;
+    }
+    cells[k] = make_float2((float)c0, (float)c1);
+  }
+  if (train)
+    for (int k = tid; k < (VF_THREADS / 32) * cpw * NB; k += blockDim.x) hist[k] = 0.0f;
+  __syncthreads();
+
+  // float64 constant of the weight: 50^D * xjac (* pref / prod k for the Gaussians)
+  double wscale = a.xjac;
+#pragma unroll
+  for (int d = 0; d < D; ++d) wscale *= 50.0;
+  if (GAUSS) {
+    double prodk = 1.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+      prodk *= SQRT_LOG2E / ((INTEG == VF_INT_SYMGAUSS) ? a.params[0] : a.params[D + d]);
+    wscale *= ((INTEG == VF_INT_SYMGAUSS) ? a.params[1] : 1.0) / prodk;
+  }
+  IntegrandConsts<float, D> kc;
+  if (!GAUSS) load_consts<D>(kc, INTEG, a.params, D);
+
+  float* my_hist = hist + (warp * cpw + ((lane * cpw) >> 5)) * NB;
+  F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
+
+  // one event from its per-dimension (bin, m) pairs
+  auto finish = [&](const int (&bins)[D], float wf, float s, const float (&x)[D]) {
+    float f;
+    if (GAUSS)
+      f = ex2_approx_ftz(-s);
+    else
+      f = eval_builtin<D>(INTEG, x, D, kc);
+    const float v = wf * f;
+    const float v2 = v * v;
+    two_sum_add(s1, v);
+    two_sum_add(s2, v2);
+    if (train) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) atomicAdd(my_hist + bins[d], v2);
+    }
+  };
+
+  const long long n = a.n_events;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long e = (long long)blockIdx.x * blockDim.x + tid;
+  if (a.u_inj == nullptr) {
+    for (; e < n; e += stride) {
+      const u64 ev = (u64)(a.ev_offset + e);
+      int bins[D];
+      float x[D];
+      float wf = 1.0f, s = 0.0f;
+#pragma unroll
+      for (int q = 0; q < (D + 3) / 4; ++q) {
+        u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+        philox4x32_10_rk(c0, c1, c2, c3, a.rk);
+        const u32 wq[4] = {c0, c1, c2, c3};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int d = 4 * q + j;
+          if (d < D) {
+            const u64 pp = (u64)(~wq[j]) * 50ull + 25ull;
+            const int i = (int)(pp >> 32);
+            const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
+            const float2 c = cells[d * VF_BINS + i];
+            const float t = fmaf(c.y, m, c.x);
+            wf = (d == 0) ? c.y : wf * c.y;
+            if (GAUSS)
+              s = fmaf(t, t, s);
+            else
+              x[d] = t;
+            bins[d] = d * VF_BINS + i;
+          }
+        }
+      }
+      finish(bins, wf, s, x);
+    }
+  } else {
+    int bad = 0;
+    for (; e < n; e += stride) {
+      const double* up = a.u_inj + e * D;
+      int bins[D];
+      float x[D];
+      float wf = 1.0f, s = 0.0f;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        // the bin in float64, bit-exact with the reference (vflow.py:117, :67)
+        const double xn = __dmul_rn(50.0, __dsub_rn(1.0, up[d]));
+        int i = (int)xn;
+        if (i < 0 || i > VF_BINS - 1) {
+          bad = 1;
+          i = i < 0 ? 0 : VF_BINS - 1;
+        }
+        const float m = (float)(1.0 + (xn - floor(xn)));
+        const float2 c = cells[d * VF_BINS + i];
+        const float t = fmaf(c.y, m, c.x);
+        wf = (d == 0) ? c.y : wf * c.y;
+        if (GAUSS)
+          s = fmaf(t, t, s);
+        else
+          x[d] = t;
+        bins[d] = d * VF_BINS + i;
+      }
+      finish(bins, wf, s, x);
+    }
+    if (bad && a.flags) atomicOr(a.flags, VF_FLAG_INDEX_RANGE);
+  }
+
+  // ---- block partials: TwoSum merges across the warp and the block, float64 row
+  __shared__ double red[2][VF_THREADS / 32];
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  if (lane == 0) {
+    red[0][warp] = (double)s1.s + (double)s1.c;
+    red[1][warp] = (double)s2.s + (double)s2.c;
+  }
+  __syncthreads();
+  const int W = 2 + NB;
+  double* row = a.partials + (long long)blockIdx.x * W;
+  if (tid == 0) {
+    double b1 = 0.0, b2 = 0.0;
+    for (int i = 0; i < VF_THREADS / 32; ++i) {
+      b1 += red[0][i];
+      b2 += red[1][i];
+    }
+    b1 *= wscale;
+    b2 *= wscale * wscale;
+    if ((!isfinite(b1) || !isfinite(b2)) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+    if (a.accumulate) {
+      row[0] += b1;
+      row[1] += b2;
+    } else {
+      row[0] = b1;
+      row[1] = b2;
+    }
+  }
+  if (train) {
+    const double s2c = wscale * wscale;
+    const int ncopies = (VF_THREADS / 32) * cpw;
+    for (int k = tid; k < NB; k += blockDim.x) {
+      double h = 0.0;
+      for (int c = 0; c < ncopies; ++c) h += (double)hist[c * NB + k];
+      h *= s2c;
+      if (a.accumulate)
+        row[2 + k] += h;
+      else
+        row[2 + k] = h;
+    }
+  }
+}
+
+}  // namespace vf
