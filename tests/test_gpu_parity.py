@@ -183,7 +183,9 @@ def test_fp64_breit_wigner_and_gauss_against_oracle():
     cases = [(6, integrands.breit_wigner(c), lambda x: oracle.integrand_breit_wigner(x, coeffs=c)),
              (5, integrands.gauss([0.3, 0.4, 0.5, 0.6, 0.7], [0.1, 0.2, 0.05, 0.15, 0.1]),
               lambda x: oracle.integrand_gauss_mu(x, [0.3, 0.4, 0.5, 0.6, 0.7], [0.1, 0.2, 0.05, 0.15, 0.1])),
-             (12, integrands.symgauss(0.2), lambda x: oracle.integrand_symgauss(x, 0.2))]
+             (12, integrands.symgauss(0.2), lambda x: oracle.integrand_symgauss(x, 0.2)),
+             (16, integrands.symgauss(0.3), lambda x: oracle.integrand_symgauss(x, 0.3)),
+             (9, integrands.prod(), oracle.integrand_prod)]
     for n_dim, dint, ofn in cases:
         inst = VegasFlow(n_dim, 50_000, verbose=False, seed=11)
         inst.compile(dint)

@@ -66,7 +66,7 @@ void fill_philox(vf::SampleArgs& a, unsigned long long seed, unsigned int call) 
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
   }
-  for (int q = 0; q < 4; ++q) a.ctr2[q] = (call << 4) | (unsigned int)q;
+  for (int q = 0; q < 8; ++q) a.ctr2[q] = (call << 4) | (unsigned int)q;
   a.ctr3 = call >> 28;
 }
 

@@ -47,7 +47,8 @@ struct SampleArgs {
   int hist_copies;          // generic kernel: 1 = one block histogram, >1 = per-warp copies;
                             // fp32 VEGAS kernel: copies per warp (1, 2, 4)
   RoundKeys rk;             // Philox round keys (seed + r W, r = 0..9), host-computed
-  unsigned int ctr2[4];     // Philox counter word 2 of 4-word block q: (call << 4) | q
+  unsigned int ctr2[8];     // Philox counter word 2 of 4-word block q: (call << 4) | q;
+                            // float64 uses ceil(D/2) <= 8 blocks, fp32 ceil(D/4) <= 4
   unsigned int ctr3;        // Philox counter word 3: call >> 28
 };
 
