@@ -55,8 +55,8 @@ extern "C" {
 #define VF_INT_JIT_BASE 1000   /* ids returned by vf_jit_integrand               */
 
 /* ---- tunables (vf_tune_set / vf_tune_get) ---------------------------------- */
-#define VF_TUNE_F32_HIST_COPIES 1 /* fp32 VEGAS histogram: 0 = exact integer buckets
-                                      (default), 1|2|4 = float atomics, copies per warp */
+#define VF_TUNE_F32_HIST_COPIES 1 /* fp32 VEGAS histogram: 0 = joint tables of dimension
+                                      pairs (default), 1|2|4 = per-dimension, copies per warp */
 
 int vf_version(void);
 const char* vf_last_error_string(void);

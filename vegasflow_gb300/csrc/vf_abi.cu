@@ -14,7 +14,7 @@
 namespace {
 
 // Tunables (vf_tune_set): histogram copies per warp of the fp32 VEGAS sampler.
-// 0 = exact integer buckets, 1|2|4 = float atomics with that many copies per warp.
+// 0 = joint pair tables, 1|2|4 = per-dimension tables with that many copies per warp.
 std::atomic<int> g_f32_hist_copies{0};
 
 thread_local char g_err[1024] = "";
@@ -90,7 +90,7 @@ int vf_version(void) { return 1; }
 int vf_tune_set(int key, int value) {
   if (key == VF_TUNE_F32_HIST_COPIES) {
     if (value != 0 && value != 1 && value != 2 && value != 4)
-      return fail(VF_ERR_ARG, "vf_tune_set: histogram layout must be 0 (integer buckets) or 1, 2, 4");
+      return fail(VF_ERR_ARG, "vf_tune_set: histogram layout must be 0 (joint pairs) or 1, 2, 4");
     g_f32_hist_copies.store(value);
     return VF_OK;
   }
@@ -208,26 +208,10 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   }
   int rc = prepare_smem(k, smem);
   if (rc) return rc;
-  // the integer-bucket histogram is exact up to 2^23 events per block: larger
-  // launches are split into consecutive sub-launches that add to the rows
-  long long per_launch = n_events;
-  if (fast && a.train && a.hist_copies == 0) {
-    const long long cap = (long long)rows * VF_F32_MAX_EVENTS_PER_BLOCK;
-    if (per_launch > cap) per_launch = cap;
-  }
-  long long done = 0;
-  do {
-    const long long m = (n_events - done < per_launch) ? n_events - done : per_launch;
-    a.n_events = m;
-    a.ev_offset = ev_offset + done;
-    a.u_inj = u_inj ? u_inj + done * n_dim : nullptr;
-    a.accumulate = (accumulate || done > 0) ? 1 : 0;
-    void* args[] = {&a};
-    const cudaError_t e =
-        cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
-    if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "vf_sample launch: %s", cudaGetErrorString(e));
-    done += m;
-  } while (done < n_events);
+  void* args[] = {&a};
+  const cudaError_t e =
+      cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "vf_sample launch: %s", cudaGetErrorString(e));
   return check_launch("vf_sample");
 }
 

@@ -19,14 +19,13 @@
 // Per event: accumulation of w f and (w f)^2 in TwoSum-compensated fp32, and
 // (when training) the (w f)^2 histogram in shared memory, in one of two layouts
 // (`hist_copies`):
-//   0   exact integer buckets (the default): (w f)^2 = m 2^(e-150) with a 24-bit
-//       mantissa m and biased exponent e; m << (e mod 16) is added with a native
-//       64-bit integer atomic to bucket e / 16 of the bin (16 buckets, bucket-major
-//       so the lanes of a warp spread over the banks).  The sums are exact and
-//       independent of the order of the additions; at the end each bin is
-//       sum_j acc[j] 2^(16 j - 150) in float64.  A bucket receives at most
-//       2^40 per event, so a block may take up to 2^23 events (checked by the host).
-//   1,2,4  float atomics into that many copies per warp (lane groups).
+//   0      joint pairs (the default): dimensions (0,1), (2,3), ... share one
+//          50 x 50 table per block, so an event makes ceil(D/2) float atomic
+//          additions instead of D, and with 2500 cells the lanes of a warp rarely
+//          collide on an address.  At the end each dimension's 50 bins are the
+//          row or column sums of its pair's table (an odd last dimension keeps a
+//          plain 50-bin table).
+//   1,2,4  per-dimension tables, that many copies per warp (lane groups).
 #pragma once
 #include "vf_sample.cuh"
 
@@ -42,17 +41,14 @@ __device__ __forceinline__ float ex2_approx_ftz(float x) {
   return y;
 }
 
-#define VF_F32_HIST_BUCKETS 16
+__host__ __device__ inline int vegas_f32_joint_floats(int D) { return (D / 2) * 2500 + (D & 1) * 50; }
 
 __host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, int train) {
   const int nb = D * VF_BINS;
-  const int hist = copies_per_warp == 0 ? VF_F32_HIST_BUCKETS * nb * 8
+  const int hist = copies_per_warp == 0 ? vegas_f32_joint_floats(D) * 4
                                         : (VF_THREADS / 32) * copies_per_warp * nb * 4;
   return nb * 8 + (train ? hist : 0);
 }
-
-// events one block may take in the integer-bucket layout without overflow
-#define VF_F32_MAX_EVENTS_PER_BLOCK (1LL << 23)
 
 template <int D, int INTEG>
 __global__ void __launch_bounds__(VF_THREADS, VF_F32_MIN_BLOCKS)
@@ -63,7 +59,7 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   constexpr double SQRT_LOG2E = 1.2011224087864498;  // sqrt(log2(e))
   float2* cells = reinterpret_cast<float2*>(smem);
   float* hist = reinterpret_cast<float*>(smem + NB * sizeof(float2));
-  unsigned long long* ihist = reinterpret_cast<unsigned long long*>(smem + NB * sizeof(float2));
+  constexpr int NP = D / 2;  // joint pairs
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
@@ -91,7 +87,7 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   }
   if (train) {
     if (cpw == 0)
-      for (int k = tid; k < VF_F32_HIST_BUCKETS * NB; k += blockDim.x) ihist[k] = 0ull;
+      for (int k = tid; k < NP * 2500 + (D & 1) * VF_BINS; k += blockDim.x) hist[k] = 0.0f;
     else
       for (int k = tid; k < (VF_THREADS / 32) * cpw * NB; k += blockDim.x) hist[k] = 0.0f;
   }
@@ -127,14 +123,12 @@ vf_vegas_f32_kernel(const SampleArgs a) {
     two_sum_add(s2, v2);
     if (train) {
       if (cpw == 0) {
-        const u32 bits = __float_as_uint(v2);
-        const u32 ex = bits >> 23;
-        const u32 mant = (bits & 0x7FFFFFu) | (ex ? 0x800000u : 0u);
-        const u32 e1 = ex ? ex : 1u;
-        const u64 val = (u64)mant << (e1 & 15u);
-        unsigned long long* hb = ihist + (e1 >> 4) * NB;
 #pragma unroll
-        for (int d = 0; d < D; ++d) atomicAdd(hb + bins[d], val);
+        for (int p = 0; p < NP; ++p)
+          atomicAdd(hist + p * 2500 + (bins[2 * p] - 2 * p * VF_BINS) * VF_BINS +
+                        (bins[2 * p + 1] - (2 * p + 1) * VF_BINS),
+                    v2);
+        if (D & 1) atomicAdd(hist + NP * 2500 + (bins[D - 1] - (D - 1) * VF_BINS), v2);
       } else {
 #pragma unroll
         for (int d = 0; d < D; ++d) atomicAdd(my_hist + bins[d], v2);
@@ -241,11 +235,15 @@ vf_vegas_f32_kernel(const SampleArgs a) {
     for (int k = tid; k < NB; k += blockDim.x) {
       double h = 0.0;
       if (cpw == 0) {
-        double scale = 7.00649232162408535e-46;  // 2^-150
-#pragma unroll
-        for (int j = 0; j < VF_F32_HIST_BUCKETS; ++j) {
-          h += (double)ihist[j * NB + k] * scale;
-          scale *= 65536.0;
+        const int d = k / VF_BINS, b = k - d * VF_BINS;
+        if (d < 2 * NP) {
+          const float* tab = hist + (d >> 1) * 2500;
+          if ((d & 1) == 0)
+            for (int c = 0; c < VF_BINS; ++c) h += (double)tab[b * VF_BINS + c];  // row sum
+          else
+            for (int r = 0; r < VF_BINS; ++r) h += (double)tab[r * VF_BINS + b];  // column sum
+        } else {
+          h = (double)hist[NP * 2500 + b];
         }
       } else {
         for (int c = 0; c < ncopies; ++c) h += (double)hist[c * NB + k];
