@@ -56,7 +56,6 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NB = D * VF_BINS;
   constexpr bool GAUSS = (INTEG == VF_INT_SYMGAUSS || INTEG == VF_INT_GAUSS);
-  constexpr double SQRT_LOG2E = 1.2011224087864498;  // sqrt(log2(e))
   float2* cells = reinterpret_cast<float2*>(smem);
   float* hist = reinterpret_cast<float*>(smem + NB * sizeof(float2));
   constexpr int NP = D / 2;  // joint pairs
@@ -66,6 +65,26 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   const bool train = a.train != 0;
   const bool limits = a.xmin != nullptr;
   const int cpw = a.hist_copies;
+
+  // ---- per-block float64 constants: Gaussian centres and k_d = sqrt(log2 e)/a_d,
+  // and the weight constant 50^D * xjac (* pref / prod k_d)
+  __shared__ double g_mu[D], g_k[D], g_wscale;
+  constexpr double SQRT_LOG2E = 1.2011224087864498;  // sqrt(log2(e))
+  if (GAUSS && tid < D) {
+    g_mu[tid] = (INTEG == VF_INT_SYMGAUSS) ? 0.5 : a.params[tid];
+    g_k[tid] = SQRT_LOG2E / ((INTEG == VF_INT_SYMGAUSS) ? a.params[0] : a.params[D + tid]);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double ws = a.xjac;
+    for (int d = 0; d < D; ++d) ws *= 50.0;
+    if (GAUSS) {
+      double prodk = 1.0;
+      for (int d = 0; d < D; ++d) prodk *= g_k[d];
+      ws *= ((INTEG == VF_INT_SYMGAUSS) ? a.params[1] : 1.0) / prodk;
+    }
+    g_wscale = ws;
+  }
 
   // ---- stage the per-bin table (float64, rounded once) and clear the histograms
   for (int k = tid; k < NB; k += blockDim.x) {
@@ -78,10 +97,8 @@ vf_vegas_f32_kernel(const SampleArgs a) {
       c1 = c1 * a.xdelta[d];
     }
     if (GAUSS) {
-      const double mu = (INTEG == VF_INT_SYMGAUSS) ? 0.5 : a.params[d];
-      const double kk = SQRT_LOG2E / ((INTEG == VF_INT_SYMGAUSS) ? a.params[0] : a.params[D + d]);
-      c0 = (c0 - mu) * kk;
-      c1 = c1 * kk;
+      c0 = (c0 - g_mu[d]) * g_k[d];
+      c1 = c1 * g_k[d];
     }
     cells[k] = make_float2((float)c0, (float)c1);
   }
@@ -93,17 +110,9 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   }
   __syncthreads();
 
-  // float64 constant of the weight: 50^D * xjac (* pref / prod k for the Gaussians)
-  double wscale = a.xjac;
-#pragma unroll
-  for (int d = 0; d < D; ++d) wscale *= 50.0;
-  if (GAUSS) {
-    double prodk = 1.0;
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-      prodk *= SQRT_LOG2E / ((INTEG == VF_INT_SYMGAUSS) ? a.params[0] : a.params[D + d]);
-    wscale *= ((INTEG == VF_INT_SYMGAUSS) ? a.params[1] : 1.0) / prodk;
-  }
+  // float64 constant of the weight (host-computed): 50^D * xjac, times
+  // pref / prod k for the Gaussian family
+  const double wscale = g_wscale;
   IntegrandConsts<float, D> kc;
   if (!GAUSS) load_consts<D>(kc, INTEG, a.params, D);
 
@@ -230,25 +239,26 @@ vf_vegas_f32_kernel(const SampleArgs a) {
     }
   }
   if (train) {
+    // marginals / copy sums in fp32 (the tables are fp32), one float64 scaling per bin
     const double s2c = wscale * wscale;
     const int ncopies = (VF_THREADS / 32) * cpw;
     for (int k = tid; k < NB; k += blockDim.x) {
-      double h = 0.0;
+      float hf = 0.0f;
       if (cpw == 0) {
         const int d = k / VF_BINS, b = k - d * VF_BINS;
         if (d < 2 * NP) {
           const float* tab = hist + (d >> 1) * 2500;
           if ((d & 1) == 0)
-            for (int c = 0; c < VF_BINS; ++c) h += (double)tab[b * VF_BINS + c];  // row sum
+            for (int c = 0; c < VF_BINS; ++c) hf += tab[b * VF_BINS + c];  // row sum
           else
-            for (int r = 0; r < VF_BINS; ++r) h += (double)tab[r * VF_BINS + b];  // column sum
+            for (int r = 0; r < VF_BINS; ++r) hf += tab[r * VF_BINS + b];  // column sum
         } else {
-          h = (double)hist[NP * 2500 + b];
+          hf = hist[NP * 2500 + b];
         }
       } else {
-        for (int c = 0; c < ncopies; ++c) h += (double)hist[c * NB + k];
+        for (int c = 0; c < ncopies; ++c) hf += hist[c * NB + k];
       }
-      h *= s2c;
+      const double h = (double)hf * s2c;
       if (a.accumulate)
         row[2 + k] += h;
       else
