@@ -130,6 +130,27 @@ int vf_consume_array_into_indices(const double* input, const int* indices, long 
                                   int result_size, double* out, int* flags, void* stream);
 
 /*
+ * One VEGAS iteration (sample, reduce, sigma, and refinement of `grid` in place
+ * when `train`) that allocates nothing.  No counterpart in the reference: it
+ * serves callers that cannot call cudaMalloc -- plugins whose host framework
+ * owns all device memory, code that must not allocate while a stream is being
+ * captured, fixed-budget deployments.  The block-partial scratch lives in a
+ * 4 MiB file-scope __device__ array inside the library (held by every GPU that
+ * loads it until exit); the caller passes only inputs (grid [n_dim][51],
+ * params) and the output res_sigma (device [2]: result, sigma).
+ *
+ * Limits: n_dim 1..16 and a built-in integrand id; xjac = 1/n_events, no
+ * integration limits, no per-event taps.  The first call on a device resolves
+ * the scratch's device address (cudaGetSymbolAddress): make that first call
+ * before any stream capture.  All calls share the scratch and it keeps the last
+ * call's contents (the state that must start at zero is cleared per call);
+ * calls that overlap on the GPU race on it and must be ordered by the caller.
+ */
+int vf_vegas_iteration_static(int precision, double* grid, int n_dim, long long n_events,
+                              unsigned long long seed, unsigned int call_ctr, int integrand,
+                              const double* params, int train, double* res_sigma, void* stream);
+
+/*
  * Process-wide tunables picked by the autotuner (no counterpart in the
  * reference, whose kernels are TensorFlow's).  Values apply to later launches.
  */

@@ -83,6 +83,12 @@ int prepare_smem(const void* kernel, int smem) {
 
 }  // namespace
 
+namespace vf {
+// Sets the calling thread's vf_last_error_string() for entry points defined in
+// other translation units.
+int set_error(int code, const char* message) { return fail(code, "%s", message); }
+}  // namespace vf
+
 extern "C" {
 
 int vf_version(void) { return 1; }

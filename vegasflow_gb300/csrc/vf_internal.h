@@ -20,6 +20,9 @@ inline const void* vegas_f32_kernel(int n_dim, int integrand) {
   return n_dim <= 8 ? vegas_f32_kernel_a(n_dim, integrand) : vegas_f32_kernel_b(n_dim, integrand);
 }
 
+// Records an error message for vf_last_error_string(); returns `code`.
+int set_error(int code, const char* message);
+
 inline int dim_bucket(int n_dim) { return n_dim <= 4 ? 4 : (n_dim <= 8 ? 8 : 16); }
 
 }  // namespace vf
