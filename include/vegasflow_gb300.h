@@ -121,6 +121,49 @@ int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int
                      double* sums_out, double* history, double* avg, int iter, int* flags,
                      void* stream);
 
+/*
+ * VEGAS+ (VegasFlowPlus, vflowplus.py:83-247).  The events of an iteration are
+ * laid out hypercube by hypercube: hypercube h (coordinates = digits of h in
+ * base n_strat, last dimension fastest, vflowplus.py:126-128) owns the events
+ * [ev_start[h], ev_start[h] + n_ev[h]); ev_start has n_hcubes + 1 entries, the
+ * last one the iteration's event count.  Both arrays live on the device and are
+ * rewritten by vf_plus_iteration_end when adaptive.
+ */
+/* Block count for the VEGAS+ kernels; partials hold rows * (2 + 50 n_dim) doubles. */
+int vf_plus_rows(int precision, int n_dim, int n_hcubes, int* rows);
+
+/*
+ * One iteration's events: generate_samples_in_hypercubes (vflowplus.py:46-80:
+ * xn = (p + u) 50 / n_strat, digest, w / n_ev[h]), the weight xjac = 1 /
+ * n_hcubes, the integrand, the per-hypercube sums ress/ress2
+ * (segment_sum, vflowplus.py:206-214) and the histogram rows.  Philox counter =
+ * the event's index within the iteration.  VF_INT_NONE samples only (taps).
+ */
+int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, int n_hcubes,
+                   const int* n_ev, const long long* ev_start, double xjac, const double* xmin,
+                   const double* xdelta, double xdeltajac, const double* u_inj,
+                   unsigned long long seed, unsigned int call_ctr, int integrand, const double* params,
+                   int train, double* ress, double* ress2, double* partials, int rows, int* ind_out,
+                   void* x_out, void* w_out, int* flags, void* stream);
+
+/* Per-hypercube sums and histogram rows from torch-evaluated f and the sampler's w, ind. */
+int vf_plus_reduce_events(int precision, const void* f, const void* w, const int* ind, const int* n_ev,
+                          const long long* ev_start, int n_dim, int n_hcubes, int train, double* ress,
+                          double* ress2, double* partials, int rows, void* stream);
+
+/*
+ * VegasFlowPlus._iteration_content (vflowplus.py:222-241): res = sum ress,
+ * sigma^2 = sum max(var, 0) / (n_ev - 1) with var = ress2 n_ev - ress^2,
+ * history/average as vf_iteration_end; when adaptive, redistribute_samples
+ * (vflowplus.py:153-163: n_ev = int(max(min_neval, var^(beta/2) N0 / 2 / sum)))
+ * and the new ev_start; when train, the grid refinement.
+ */
+int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, long long* ev_start,
+                          int n_hcubes, int adaptive, int min_neval, double init_calls,
+                          const double* partials, int rows, int n_dim, int train, double alpha,
+                          double beta, double* grid, double* hist_out, double* arr_var_out,
+                          double* history, double* avg, int iter, int* flags, void* stream);
+
 /* VegasFlow.refine_grid(arr_res2) (vflow.py:349-362): hist [n_dim][50]. */
 int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, int* flags,
                    void* stream);

@@ -132,3 +132,25 @@ def test_integrand_torch_forms_match_oracle():
     np.testing.assert_allclose(integrands.breit_wigner(c)(t).numpy(),
                                oracle.integrand_breit_wigner(x, coeffs=c), rtol=1e-13)
     np.testing.assert_allclose(integrands.prod()(t).numpy(), oracle.integrand_prod(x), rtol=1e-15)
+
+
+def test_plus_stratification_matches_reference(golden):
+    """vflowplus.py:105-139 (float32 powers) against the reference's own values."""
+    from vegasflow_gb300.vflowplus import stratification
+
+    for row in golden["strat/table"]:
+        n_dim, n_ev, adapt, adapt_eff, n_strat, n_h, min_neval, n_events = (int(v) for v in row)
+        assert stratification(n_dim, n_ev, bool(adapt)) == (bool(adapt_eff), n_strat, n_h, min_neval,
+                                                            n_events), row
+
+
+def test_plus_host_state():
+    from vegasflow_gb300 import VegasFlowPlus
+
+    inst = VegasFlowPlus(6, 2_000_000, adaptive=True, device="cpu")
+    assert inst.n_hypercubes == 4096 and inst.min_neval_hcube == 244 and inst.n_events == 999_424
+    assert inst.xjac == 1.0 / 4096
+    assert int(inst._ev_start[-1]) == inst.n_events and inst._ev_start[1] == 244
+    assert inst._events_limit == 2_000_000
+    inst2 = VegasFlowPlus(14, 100_000, adaptive=True, device="cpu")
+    assert inst2._adaptive is False and inst2.n_hypercubes == 1

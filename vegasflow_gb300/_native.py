@@ -63,6 +63,12 @@ SIGNATURES = {
     "vf_consume_array_into_indices": [_P, _P, _LL, _I, _P, _P, _P],
     "vf_issue_probe": [_P, _I, _I, _P, _P],
     "vf_vegas_iteration_static": [_I, _P, _I, _LL, _U64, _U32, _I, _P, _I, _P, _P],
+    "vf_plus_rows": [_I, _I, _I, _P],
+    "vf_plus_sample": [_I, _P, _I, _I, _I, _P, _P, _D, _P, _P, _D, _P, _U64, _U32, _I, _P, _I, _P, _P,
+                       _P, _I, _P, _P, _P, _P, _P],
+    "vf_plus_reduce_events": [_I, _P, _P, _P, _P, _P, _I, _I, _I, _P, _P, _P, _I, _P],
+    "vf_plus_iteration_end": [_P, _P, _P, _P, _I, _I, _I, _D, _P, _I, _I, _I, _D, _D, _P, _P, _P, _P,
+                              _P, _I, _P, _P],
     "vf_tune_set": [_I, _I],
     "vf_tune_get": [_I, _P],
 }

@@ -1,0 +1,196 @@
+// VEGAS+ entry points (vf_plus_*) and the ahead-of-time instantiations of the
+// stratified sampler.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "vegasflow_gb300.h"
+#include "vf_internal.h"
+#include "vf_plus.cuh"
+
+namespace {
+
+template <typename Real, int DMAX>
+const void* pick(int integrand) {
+  switch (integrand) {
+    case VF_INT_NONE: return (const void*)vf::vf_plus_kernel<Real, DMAX, VF_INT_NONE>;
+    case VF_INT_SYMGAUSS: return (const void*)vf::vf_plus_kernel<Real, DMAX, VF_INT_SYMGAUSS>;
+    case VF_INT_GAUSS: return (const void*)vf::vf_plus_kernel<Real, DMAX, VF_INT_GAUSS>;
+    case VF_INT_BREIT_WIGNER: return (const void*)vf::vf_plus_kernel<Real, DMAX, VF_INT_BREIT_WIGNER>;
+    case VF_INT_PROD: return (const void*)vf::vf_plus_kernel<Real, DMAX, VF_INT_PROD>;
+    case VF_INT_SUM: return (const void*)vf::vf_plus_kernel<Real, DMAX, VF_INT_SUM>;
+    default: return nullptr;
+  }
+}
+
+const void* plus_kernel(int precision, int n_dim, int integrand) {
+  const int dmax = vf::dim_bucket(n_dim);
+  if (precision == VF_PREC_F64) {
+    if (dmax == 4) return pick<double, 4>(integrand);
+    if (dmax == 8) return pick<double, 8>(integrand);
+    return pick<double, 16>(integrand);
+  }
+  if (dmax == 4) return pick<float, 4>(integrand);
+  if (dmax == 8) return pick<float, 8>(integrand);
+  return pick<float, 16>(integrand);
+}
+
+int err(int code, const char* msg) { return vf::set_error(code, msg); }
+
+int launched(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    return err(VF_ERR_LAUNCH, buf);
+  }
+  return VF_OK;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vf_plus_rows(int precision, int n_dim, int n_hcubes, int* rows) {
+  if (!rows || n_dim < 1 || n_dim > VF_MAX_DIM || n_hcubes < 1)
+    return err(VF_ERR_ARG, "vf_plus_rows: bad arguments");
+  const int sms = sm_count();
+  if (sms <= 0) return err(VF_ERR_CUDA, "vf_plus_rows: no CUDA device");
+  // one warp per hypercube, at most 4 blocks per SM of 8 warps
+  int need = (n_hcubes + VF_THREADS / 32 - 1) / (VF_THREADS / 32);
+  const int cap = 4 * sms;
+  *rows = need < cap ? need : cap;
+  (void)precision;
+  return VF_OK;
+}
+
+int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, int n_hcubes,
+                   const int* n_ev, const long long* ev_start, double xjac, const double* xmin,
+                   const double* xdelta, double xdeltajac, const double* u_inj,
+                   unsigned long long seed, unsigned int call_ctr, int integrand, const double* params,
+                   int train, double* ress, double* ress2, double* partials, int rows, int* ind_out,
+                   void* x_out, void* w_out, int* flags, void* stream) {
+  if (precision != VF_PREC_F64 && precision != VF_PREC_F32) return err(VF_ERR_ARG, "vf_plus_sample: precision");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_plus_sample: n_dim must be 1..16");
+  if (!grid || !n_ev || !ev_start || n_strat < 1 || n_hcubes < 1 || rows < 1)
+    return err(VF_ERR_ARG, "vf_plus_sample: NULL buffer or bad stratification");
+  if ((xmin == nullptr) != (xdelta == nullptr)) return err(VF_ERR_ARG, "vf_plus_sample: xmin/xdelta");
+  if (integrand < VF_INT_NONE || integrand > VF_INT_SUM) return err(VF_ERR_ARG, "vf_plus_sample: integrand");
+  if (integrand != VF_INT_NONE && (!ress || !ress2 || !partials))
+    return err(VF_ERR_ARG, "vf_plus_sample: ress/ress2/partials required when evaluating");
+  if ((integrand == VF_INT_SYMGAUSS || integrand == VF_INT_GAUSS || integrand == VF_INT_BREIT_WIGNER) && !params)
+    return err(VF_ERR_ARG, "vf_plus_sample: integrand needs params");
+  const void* k = plus_kernel(precision, n_dim, integrand);
+  if (!k) return err(VF_ERR_UNSUPPORTED, "vf_plus_sample: no kernel");
+  vf::PlusArgs a;
+  a.grid = grid;
+  a.n_ev = n_ev;
+  a.ev_start = ev_start;
+  a.xmin = xmin;
+  a.xdelta = xdelta;
+  a.u_inj = u_inj;
+  a.params = params;
+  a.ress = ress;
+  a.ress2 = ress2;
+  a.partials = partials;
+  a.ind_out = ind_out;
+  a.x_out = x_out;
+  a.w_out = w_out;
+  a.flags = flags;
+  a.xjac = xjac;
+  a.xdeltajac = xmin ? xdeltajac : 1.0;
+  a.n_dim = n_dim;
+  a.n_strat = n_strat;
+  a.n_hcubes = n_hcubes;
+  a.train = train ? 1 : 0;
+  unsigned int k0 = (unsigned int)seed, k1 = (unsigned int)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    a.rk.k0[r] = k0;
+    a.rk.k1[r] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  for (int q = 0; q < 8; ++q) a.ctr2[q] = (call_ctr << 4) | (unsigned int)q;
+  a.ctr3 = call_ctr >> 28;
+  const int smem = vf::plus_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, a.train);
+  void* args[] = {&a};
+  const cudaError_t e = cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
+  if (e != cudaSuccess) return err(VF_ERR_LAUNCH, cudaGetErrorString(e));
+  return launched("vf_plus_sample");
+}
+
+int vf_plus_reduce_events(int precision, const void* f, const void* w, const int* ind, const int* n_ev,
+                          const long long* ev_start, int n_dim, int n_hcubes, int train, double* ress,
+                          double* ress2, double* partials, int rows, void* stream) {
+  if (!f || !w || !n_ev || !ev_start || !ress || !ress2 || !partials || rows < 1 || n_hcubes < 1)
+    return err(VF_ERR_ARG, "vf_plus_reduce_events: NULL buffer");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_plus_reduce_events: n_dim");
+  if (train && !ind) return err(VF_ERR_ARG, "vf_plus_reduce_events: ind required when train");
+  vf::PlusReduceArgs a;
+  a.f = f;
+  a.w = w;
+  a.ind = ind;
+  a.n_ev = n_ev;
+  a.ev_start = ev_start;
+  a.ress = ress;
+  a.ress2 = ress2;
+  a.partials = partials;
+  a.n_dim = n_dim;
+  a.n_hcubes = n_hcubes;
+  a.train = train ? 1 : 0;
+  const int smem = n_dim * VF_BINS * 8;
+  if (precision == VF_PREC_F64)
+    vf::vf_plus_reduce_kernel<double><<<rows, VF_THREADS, smem, (cudaStream_t)stream>>>(a);
+  else if (precision == VF_PREC_F32)
+    vf::vf_plus_reduce_kernel<float><<<rows, VF_THREADS, smem, (cudaStream_t)stream>>>(a);
+  else
+    return err(VF_ERR_ARG, "vf_plus_reduce_events: precision");
+  return launched("vf_plus_reduce_events");
+}
+
+int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, long long* ev_start,
+                          int n_hcubes, int adaptive, int min_neval, double init_calls,
+                          const double* partials, int rows, int n_dim, int train, double alpha,
+                          double beta, double* grid, double* hist_out, double* arr_var_out,
+                          double* history, double* avg, int iter, int* flags, void* stream) {
+  if (!ress || !ress2 || !n_ev || !ev_start || !history || !avg || n_hcubes < 1 || iter < 0)
+    return err(VF_ERR_ARG, "vf_plus_iteration_end: NULL buffer");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_plus_iteration_end: n_dim");
+  if ((train || hist_out) && (!partials || rows < 1)) return err(VF_ERR_ARG, "vf_plus_iteration_end: partials");
+  if (train && !grid) return err(VF_ERR_ARG, "vf_plus_iteration_end: grid required when train");
+  if (adaptive && min_neval < 1) return err(VF_ERR_ARG, "vf_plus_iteration_end: min_neval");
+  vf::PlusEndArgs a;
+  a.ress = ress;
+  a.ress2 = ress2;
+  a.n_ev = n_ev;
+  a.ev_start = ev_start;
+  a.arr_var = arr_var_out;
+  a.partials = partials;
+  a.grid = grid;
+  a.hist_out = hist_out;
+  a.history = history;
+  a.avg = avg;
+  a.flags = flags;
+  a.init_calls = init_calls;
+  a.alpha = alpha;
+  a.beta = beta;
+  a.n_hcubes = n_hcubes;
+  a.min_neval = min_neval;
+  a.adaptive = adaptive ? 1 : 0;
+  a.rows = rows;
+  a.n_dim = n_dim;
+  a.train = train ? 1 : 0;
+  a.iter = iter;
+  const int blocks = (a.train || hist_out) ? n_dim + 1 : 1;
+  vf::vf_plus_iteration_end_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(a);
+  return launched("vf_plus_iteration_end");
+}
+
+}  // extern "C"

@@ -1,0 +1,390 @@
+// VEGAS+ (importance + adaptive stratified sampling) kernels.
+//
+// Events are laid out hypercube by hypercube: hypercube h owns the events
+// [ev_start[h], ev_start[h] + n_ev[h]) of the iteration, with ev_start the
+// exclusive prefix sum of n_ev (kept on the device, rebuilt by the
+// reallocation step).  One warp processes one hypercube at a time, so the
+// per-hypercube sums are warp reductions written by one lane (deterministic).
+// Hypercube h has coordinates p_d = digit d of h in base n_strat, the last
+// dimension fastest (the itertools.product order of vflowplus.py:126-128).
+#pragma once
+#include "vf_refine.cuh"
+#include "vf_sample.cuh"
+
+namespace vf {
+
+struct PlusArgs {
+  const double* grid;        // [D][51]
+  const int* n_ev;           // [H]
+  const long long* ev_start; // [H + 1]
+  const double* xmin;        // nullable [D]
+  const double* xdelta;      // nullable [D]
+  const double* u_inj;       // nullable [n_events][D] (post-affine uniforms, event order)
+  const double* params;
+  double* ress;              // [H]: sum of w f per hypercube (nullable when sampling only)
+  double* ress2;             // [H]: sum of (w f)^2
+  double* partials;          // [rows][2 + 50 D]: block sums and histogram
+  int* ind_out;              // nullable taps, indexed by event
+  void* x_out;
+  void* w_out;
+  int* flags;
+  double xjac;               // 1 / n_hypercubes (vflowplus.py:139, :144-146)
+  double xdeltajac;
+  int n_dim;
+  int n_strat;
+  int n_hcubes;
+  int train;
+  RoundKeys rk;
+  unsigned int ctr2[8];
+  unsigned int ctr3;
+};
+
+__host__ __device__ inline int plus_smem_bytes(int real_size, int D, int train) {
+  return D * VF_EDGES * 8 + (train ? D * VF_BINS * real_size : 0) + 2 * VF_MAX_DIM * 8;
+}
+
+template <typename Real, int DMAX, int INTEG>
+__global__ void __launch_bounds__(VF_THREADS) vf_plus_kernel(const PlusArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int D = a.n_dim;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr bool evaluate = (INTEG != VF_INT_NONE);
+  const bool fill_hist = evaluate && a.train;
+  const int nb = D * VF_BINS;
+  double* edges = reinterpret_cast<double*>(smem);
+  Real* hist = reinterpret_cast<Real*>(smem + D * VF_EDGES * 8);
+  for (int k = tid; k < D * VF_EDGES; k += blockDim.x) edges[k] = a.grid[k];
+  if (fill_hist)
+    for (int k = tid; k < nb; k += blockDim.x) hist[k] = (Real)0;
+  __syncthreads();
+
+  IntegrandConsts<Real, DMAX> kc;
+  load_consts<DMAX>(kc, INTEG, a.params, D);
+  const bool limits = a.xmin != nullptr;
+  const double inv_strat = 1.0 / (double)a.n_strat;
+  int bad = 0;
+  double blk1 = 0.0, blk2 = 0.0;  // this warp's contribution to the block row (lane 0)
+
+  const int gwarp = blockIdx.x * (blockDim.x >> 5) + warp;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int h = gwarp; h < a.n_hcubes; h += nwarps) {
+    // coordinates of hypercube h (last dimension fastest)
+    int p[DMAX];
+    {
+      int rem = h;
+#pragma unroll
+      for (int d = DMAX - 1; d >= 0; --d)
+        if (d < D) {
+          p[d] = rem % a.n_strat;
+          rem /= a.n_strat;
+        }
+    }
+    const int nev = a.n_ev[h];
+    const long long e0 = a.ev_start[h];
+    double s1 = 0.0, s2 = 0.0;
+    for (int j = lane; j < nev; j += 32) {
+      const long long e = e0 + j;
+      double u[DMAX];
+      if (a.u_inj != nullptr) {
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d)
+          if (d < D) u[d] = a.u_inj[e * D + d];
+      } else {
+        // 53-bit uniforms through the TECH_CUT affine (both precisions: the
+        // stratified map needs the full resolution of p + u)
+#pragma unroll
+        for (int q = 0; q < (DMAX + 1) / 2; ++q)
+          if (2 * q < D) {
+            u32 c0 = (u32)e, c1 = (u32)((u64)e >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+            philox4x32_10_rk(c0, c1, c2, c3, a.rk);
+            u[2 * q] = tech_cut(u53(c0, c1));
+            if (2 * q + 1 < DMAX) u[2 * q + 1] = tech_cut(u53(c2, c3));
+          }
+      }
+      Real x[DMAX];
+      int ind[DMAX];
+      double w = 1.0;
+#pragma unroll
+      for (int d = 0; d < DMAX; ++d)
+        if (d < D) {
+          double xn;
+          if constexpr (sizeof(Real) == 8) {
+            // vflowplus.py:72: (p + u) * 50 / n_strat, three roundings
+            xn = __ddiv_rn(__dmul_rn(__dadd_rn((double)p[d], u[d]), 50.0), (double)a.n_strat);
+          } else {
+            xn = ((double)p[d] + u[d]) * 50.0 * inv_strat;
+          }
+          int i = (int)xn;
+          if (i < 0 || i > VF_BINS - 1) {
+            bad = 1;
+            i = i < 0 ? 0 : VF_BINS - 1;
+          }
+          const double lo = edges[d * VF_EDGES + i];
+          const double dl = __dsub_rn(edges[d * VF_EDGES + i + 1], lo);
+          const double aux = __dsub_rn(xn, floor(xn));
+          x[d] = (Real)__dadd_rn(lo, __dmul_rn(dl, aux));
+          const double fac = __dmul_rn(dl, 50.0);
+          w = (d == 0) ? fac : __dmul_rn(w, fac);
+          ind[d] = i;
+        }
+      w = __ddiv_rn(w, (double)nev);   // vflowplus.py:77
+      w = __dmul_rn(w, a.xjac);        // monte_carlo.py:270
+      if (limits) {
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d)
+          if (d < D) x[d] = (Real)__dadd_rn(a.xmin[d], __dmul_rn((double)x[d], a.xdelta[d]));
+        w = __dmul_rn(w, a.xdeltajac);
+      }
+      if (evaluate) {
+        const double f = (double)eval_builtin<DMAX>(INTEG, x, D, kc);
+        const double tmp = __dmul_rn(w, f);  // vflowplus.py:209
+        const double tmp2 = __dmul_rn(tmp, tmp);
+        s1 += tmp;
+        s2 += tmp2;
+        if (fill_hist) {
+#pragma unroll
+          for (int d = 0; d < DMAX; ++d)
+            if (d < D) atomicAdd(hist + d * VF_BINS + ind[d], (Real)tmp2);
+        }
+      }
+      if (a.ind_out) {
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d)
+          if (d < D) a.ind_out[e * D + d] = ind[d];
+      }
+      if (a.x_out) {
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d)
+          if (d < D) reinterpret_cast<Real*>(a.x_out)[e * D + d] = x[d];
+      }
+      if (a.w_out) reinterpret_cast<Real*>(a.w_out)[e] = (Real)w;
+    }
+    if (evaluate) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      }
+      if (lane == 0) {
+        a.ress[h] = s1;   // segment_sum, vflowplus.py:213-214
+        a.ress2[h] = s2;
+        blk1 += s1;
+        blk2 += s2;
+      }
+    }
+  }
+  if (bad && a.flags) atomicOr(a.flags, VF_FLAG_INDEX_RANGE);
+  if (!evaluate) return;
+  __shared__ double red[2][VF_THREADS / 32];
+  if (lane == 0) {
+    red[0][warp] = blk1;
+    red[1][warp] = blk2;
+  }
+  __syncthreads();
+  double* row = a.partials + (long long)blockIdx.x * (2 + nb);
+  if (tid == 0) {
+    double b1 = 0.0, b2 = 0.0;
+    for (int i = 0; i < VF_THREADS / 32; ++i) {
+      b1 += red[0][i];
+      b2 += red[1][i];
+    }
+    row[0] = b1;
+    row[1] = b2;
+  }
+  if (fill_hist)
+    for (int k = tid; k < nb; k += blockDim.x) row[2 + k] = (double)hist[k];
+}
+
+// Torch-evaluated integrands: per-hypercube sums and histogram from f, w, ind.
+struct PlusReduceArgs {
+  const void* f;             // [n_events] (Real)
+  const void* w;             // [n_events] (Real)
+  const int* ind;            // [n_events][D]
+  const int* n_ev;
+  const long long* ev_start;
+  double* ress;
+  double* ress2;
+  double* partials;
+  int n_dim;
+  int n_hcubes;
+  int train;
+};
+
+template <typename Real>
+__global__ void __launch_bounds__(VF_THREADS) vf_plus_reduce_kernel(const PlusReduceArgs a) {
+  extern __shared__ double hsm[];
+  const int D = a.n_dim, nb = D * VF_BINS;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (a.train)
+    for (int k = tid; k < nb; k += blockDim.x) hsm[k] = 0.0;
+  __syncthreads();
+  const Real* f = reinterpret_cast<const Real*>(a.f);
+  const Real* w = reinterpret_cast<const Real*>(a.w);
+  const int gwarp = blockIdx.x * (blockDim.x >> 5) + warp;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int h = gwarp; h < a.n_hcubes; h += nwarps) {
+    const int nev = a.n_ev[h];
+    const long long e0 = a.ev_start[h];
+    double s1 = 0.0, s2 = 0.0;
+    for (int j = lane; j < nev; j += 32) {
+      const long long e = e0 + j;
+      const double tmp = (double)w[e] * (double)f[e];
+      const double tmp2 = tmp * tmp;
+      s1 += tmp;
+      s2 += tmp2;
+      if (a.train)
+        for (int d = 0; d < D; ++d) {
+          const int b = a.ind[e * D + d];
+          if (b >= 0 && b < VF_BINS) atomicAdd(&hsm[d * VF_BINS + b], tmp2);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) {
+      a.ress[h] = s1;
+      a.ress2[h] = s2;
+    }
+  }
+  __syncthreads();
+  double* row = a.partials + (long long)blockIdx.x * (2 + nb);
+  if (tid == 0) {
+    row[0] = 0.0;
+    row[1] = 0.0;
+  }
+  if (a.train)
+    for (int k = tid; k < nb; k += blockDim.x) row[2 + k] = hsm[k];
+}
+
+// Iteration end of VEGAS+ (vflowplus.py:222-241): result and sigma from the
+// per-hypercube sums, the adaptive reallocation (vflowplus.py:153-163) with the
+// new prefix sum, and -- in the other blocks -- the grid refinement.
+struct PlusEndArgs {
+  const double* ress;
+  const double* ress2;
+  int* n_ev;                 // [H], rewritten when adaptive
+  long long* ev_start;       // [H + 1], rewritten when adaptive
+  double* arr_var;           // nullable [H] out: ress2 n_ev - ress^2
+  const double* partials;    // histogram rows
+  double* grid;
+  double* hist_out;
+  double* history;           // [iter][2]
+  double* avg;               // [5]
+  int* flags;
+  double init_calls;         // N0, the constructor's n_events
+  double alpha;
+  double beta;
+  int n_hcubes;
+  int min_neval;
+  int adaptive;
+  int rows;
+  int n_dim;
+  int train;
+  int iter;
+};
+
+__global__ void __launch_bounds__(256) vf_plus_iteration_end_kernel(const PlusEndArgs a) {
+  const int t = threadIdx.x;
+  const int D = a.n_dim;
+  const int H = a.n_hcubes;
+  const int W = 2 + VF_BINS * D;
+  __shared__ double part[4][64];
+  __shared__ double hsm[VF_BINS];
+  if ((a.train || a.hist_out) && (int)blockIdx.x < D) {
+    const int d = blockIdx.x;
+    const int c = t & 63, r0 = t >> 6;
+    double s = 0.0;
+    if (c < VF_BINS)
+      for (int r = r0; r < a.rows; r += 4) s += a.partials[(long long)r * W + 2 + d * VF_BINS + c];
+    part[r0][c] = s;
+    __syncthreads();
+    if (t < VF_BINS) {
+      const double v = ((part[0][t] + part[1][t]) + part[2][t]) + part[3][t];
+      hsm[t] = v;
+      if (a.hist_out) a.hist_out[d * VF_BINS + t] = v;
+    }
+    __syncthreads();
+    if (a.train) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
+    return;
+  }
+  __shared__ double red[3][256];
+  __shared__ double s_sum_damped;
+  __shared__ long long scan[256];
+  // res = sum ress, sigma^2 = sum max(var, 0) / (n_ev - 1)   (vflowplus.py:230-233)
+  double r1 = 0.0, r2 = 0.0, r3 = 0.0;
+  for (int h = t; h < H; h += blockDim.x) {
+    const double nev = (double)a.n_ev[h];
+    const double var = __dsub_rn(__dmul_rn(a.ress2[h], nev), __dmul_rn(a.ress[h], a.ress[h]));
+    if (a.arr_var) a.arr_var[h] = var;
+    r1 += a.ress[h];
+    r2 += fmax(var, 0.0) / (nev - 1.0);
+    if (a.adaptive) r3 += pow(var, a.beta / 2.0);  // NaN for var < 0, as the reference
+  }
+  red[0][t] = r1;
+  red[1][t] = r2;
+  red[2][t] = r3;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (t < o) {
+      red[0][t] += red[0][t + o];
+      red[1][t] += red[1][t + o];
+      red[2][t] += red[2][t + o];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    const double res = red[0][0];
+    const double sigma = sqrt(red[1][0]);
+    double* hrow = a.history + (long long)a.iter * 2;
+    hrow[0] = res;
+    hrow[1] = sigma;
+    const double wgt = 1.0 / __dmul_rn(sigma, sigma);
+    a.avg[0] = __dadd_rn(a.avg[0], __dmul_rn(res, wgt));
+    a.avg[1] = __dadd_rn(a.avg[1], wgt);
+    const double mean = a.avg[0] / a.avg[1];
+    a.avg[2] = mean;
+    a.avg[3] = sqrt(1.0 / a.avg[1]);
+    double chi2 = 0.0;
+    for (int i = 0; i <= a.iter; ++i) {
+      const double r = a.history[2 * i], sg = a.history[2 * i + 1];
+      chi2 += (r - mean) * (r - mean) / (sg * sg);
+    }
+    a.avg[4] = a.iter > 0 ? chi2 / a.iter : 0.0;
+    if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+    s_sum_damped = red[2][0];
+  }
+  __syncthreads();
+  if (!a.adaptive) return;
+  // vflowplus.py:157-163: n_ev = int(max(min_neval, d^(beta/2) N0 / 2 / sum d))
+  const double sum_d = s_sum_damped;
+  // new counts, then an exclusive prefix sum in chunks of blockDim
+  long long carry = 0;
+  for (int base = 0; base < H; base += blockDim.x) {
+    const int h = base + t;
+    long long v = 0;
+    if (h < H) {
+      double var = __dsub_rn(__dmul_rn(a.ress2[h], (double)a.n_ev[h]), __dmul_rn(a.ress[h], a.ress[h]));
+      const double dmp = pow(var, a.beta / 2.0);
+      const double nn = fmax((double)a.min_neval, dmp * a.init_calls / 2.0 / sum_d);
+      v = (long long)(int)nn;
+    }
+    __syncthreads();  // everyone has read n_ev[h] before it is rewritten
+    if (h < H) a.n_ev[h] = (int)v;
+    scan[t] = v;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {  // inclusive Hillis-Steele scan
+      const long long add = t >= o ? scan[t - o] : 0;
+      __syncthreads();
+      scan[t] += add;
+      __syncthreads();
+    }
+    if (h < H) a.ev_start[h] = carry + scan[t] - v;
+    carry += scan[blockDim.x - 1];
+    __syncthreads();
+  }
+  if (t == 0) a.ev_start[H] = carry;
+}
+
+}  // namespace vf
