@@ -326,7 +326,7 @@ def main():
         "fp64_plain": {"value": value64, "unit": "events/s", "ms_per_step": 1e3 * total64 / K,
                        "sampler_ms": 1e3 * float(s64.mean())},
         "fp32_over_fp64": value / value64,
-        "roofline": {"bound": "issue", "kernel": "vf_sample_kernel<float,8,SYMGAUSS>",
+        "roofline": {"bound": "issue", "kernel": "vf_vegas_f32_kernel<8,SYMGAUSS>",
                      "achieved": achieved / 1e9, "peak": issue_peak / 1e9, "unit": "Gwarp-instr/s",
                      "frac": achieved / issue_peak, "traffic": None,
                      "per_event_instr": INSTR_PER_EVENT_FP32_D8,
