@@ -56,6 +56,10 @@ L2_FLUSH_BYTES = 512 << 20
 #   loop control                                                                        3
 INSTR_PER_EVENT_FP32_D8 = 208
 
+# DRAM traffic of one fp32 sampler launch (grid, parameters; the partial rows stay
+# in L2), from one ncu capture of a 1e7-event launch: 49.4 KB read, 0 written.
+SAMPLER_DRAM_BYTES = 49408
+
 
 def _parse():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
@@ -328,7 +332,10 @@ def main():
         "fp32_over_fp64": value / value64,
         "roofline": {"bound": "issue", "kernel": "vf_vegas_f32_kernel<8,SYMGAUSS>",
                      "achieved": achieved / 1e9, "peak": issue_peak / 1e9, "unit": "Gwarp-instr/s",
-                     "frac": achieved / issue_peak, "traffic": None,
+                     "frac": achieved / issue_peak, "traffic": SAMPLER_DRAM_BYTES,
+                     "traffic_note": "DRAM bytes per launch (ncu dram__bytes_read.sum + "
+                                     "dram__bytes_write.sum on a 1e7-event launch); the kernel "
+                                     "streams no per-event data, so this does not grow with events",
                      "per_event_instr": INSTR_PER_EVENT_FP32_D8,
                      "peak_source": "measured in this run: vf_issue_probe (independent FFMA chains)",
                      "sampler_ms": 1e3 * samp_mean},
