@@ -1,0 +1,94 @@
+"""Batched VEGAS (one persistent launch per iteration over many integrals):
+alone vs in the mix, CUDA-graph replay vs eager launches, and the 1,024-integral
+workload against the exact integrals."""
+
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from vegasflow_gb300 import integrands
+from vegasflow_gb300.batch import VegasBatch, c4_specs
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed_specs():
+    rng = np.random.default_rng(1)
+    c = rng.random(5)
+    return [
+        (8, 300_000, integrands.symgauss(0.1)),
+        (3, 70_000, integrands.gauss([0.4, 0.5, 0.6], [0.1, 0.15, 0.2])),
+        (6, 200_000, integrands.breit_wigner(c)),
+        (16, 150_000, integrands.symgauss(0.3)),
+        (5, 20_000, integrands.prod()),
+        (1, 10_000, integrands.gauss([0.45], [0.08])),
+        (11, 250_000, integrands.gauss(rng.uniform(0.3, 0.7, 11), rng.uniform(0.05, 0.2, 11))),
+    ]
+
+
+def _exact(d, spec):
+    f = spec
+    if f.__name__ == "symgauss":
+        return oracle.symgauss_exact(d, f.params(d)[0])
+    if f.__name__ == "gauss":
+        p = f.params(d)
+        return oracle.gauss_mu_exact(p[:d], p[d:])
+    if f.__name__ == "breit_wigner":
+        p = f.params(d)
+        return oracle.breit_wigner_exact(d, coeffs=p[2:])
+    if f.__name__ == "prod":
+        return 0.5 ** d
+    raise KeyError(f.__name__)
+
+
+def test_alone_equals_in_the_mix():
+    """Every integral alone (same seed, same stream id) against the full batch:
+    iteration 1 identical to rounding, later iterations to fp32 histogram rounding."""
+    specs = _mixed_specs()
+    mix = VegasBatch(specs, seed=77)
+    mix.run(3)
+    h_mix = mix.history_host()
+    m_mix, s_mix, _, flags = mix.results()
+    assert flags == 0
+    for i, spec in enumerate(specs):
+        alone = VegasBatch([spec], seed=77, stream_ids=[i])
+        alone.run(3)
+        h = alone.history_host()[0]
+        np.testing.assert_allclose(h[0], h_mix[i, 0], rtol=1e-12)
+        np.testing.assert_allclose(h, h_mix[i], rtol=1e-5)
+
+
+def test_graph_replay_equals_eager():
+    specs = _mixed_specs()
+    eager = VegasBatch(specs, seed=5)
+    eager.run(4)
+    graphed = VegasBatch(specs, seed=5)
+    graphed.run(4, graph=True)
+    np.testing.assert_allclose(graphed.history_host()[:, 0], eager.history_host()[:, 0], rtol=1e-12)
+    np.testing.assert_allclose(graphed.history_host(), eager.history_host(), rtol=1e-5)
+
+
+def test_mixed_batch_against_exact():
+    specs = _mixed_specs()
+    b = VegasBatch(specs, seed=3)
+    b.run(6, graph=True)
+    mean, sigma, chi2, flags = b.results()
+    for i, (d, n, f) in enumerate(specs):
+        ex = _exact(d, f)
+        assert abs(mean[i] - ex) < 5 * sigma[i], (i, f.__name__, mean[i], sigma[i], ex)
+
+
+def test_c4_1024_integrals():
+    """C4: 1,024 Gaussians, dims 2-16, 1e4-1e7 events, 5 graph-replayed iterations."""
+    specs = c4_specs()
+    b = VegasBatch(specs, seed=11)
+    b.run(5, graph=True)
+    mean, sigma, chi2, flags = b.results()
+    exact = np.array([_exact(d, f) for d, _, f in specs])
+    pulls = (mean - exact) / sigma
+    assert flags == 0
+    assert np.all(np.isfinite(pulls))
+    assert np.max(np.abs(pulls)) < 6.0, np.max(np.abs(pulls))
+    assert abs(np.mean(pulls)) < 0.2 and 0.7 < math.sqrt(np.mean(pulls ** 2)) < 1.4

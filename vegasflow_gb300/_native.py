@@ -69,6 +69,10 @@ SIGNATURES = {
     "vf_plus_reduce_events": [_I, _P, _P, _P, _P, _P, _I, _I, _I, _P, _P, _P, _I, _P],
     "vf_plus_iteration_end": [_P, _P, _P, _P, _I, _I, _I, _D, _P, _I, _I, _I, _D, _D, _P, _P, _P, _P,
                               _P, _I, _P, _P],
+    "vf_batch_blocks": [_I, _P, _P],
+    "vf_batch_sample": [_P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],
+    "vf_batch_iteration_end": [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P],
+    "vf_batch_advance": [_P, _P, _P, _P],
     "vf_tune_set": [_I, _I],
     "vf_tune_get": [_I, _P],
 }

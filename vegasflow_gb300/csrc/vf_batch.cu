@@ -1,0 +1,128 @@
+// Batched-VEGAS entry points (vf_batch_*): many integrals per launch.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+
+#include "vegasflow_gb300.h"
+#include "vf_batch.cuh"
+#include "vf_internal.h"
+
+static_assert(sizeof(vf_batch_item) == sizeof(vf::BatchItem), "vf_batch_item layout");
+
+namespace {
+
+int err(int code, const char* msg) { return vf::set_error(code, msg); }
+
+int launched(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    return err(VF_ERR_LAUNCH, buf);
+  }
+  return VF_OK;
+}
+
+// Raise the sampler's dynamic shared-memory limit once per size (a no-op
+// afterwards, so launches inside a stream capture make no attribute calls).
+std::atomic<int> g_smem_set{0};
+cudaError_t set_smem(int smem) {
+  if (smem <= g_smem_set.load()) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(vf::vf_batch_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) g_smem_set.store(smem);
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vf_batch_blocks(int max_dim, int* blocks, int* smem_bytes) {
+  if (!blocks || max_dim < 1 || max_dim > VF_MAX_DIM) return err(VF_ERR_ARG, "vf_batch_blocks: max_dim");
+  const int smem = vf::batch_smem_bytes(max_dim);
+  cudaError_t e = set_smem(smem);
+  if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
+  // load the batch kernels now, so that a later stream capture launches only
+  cudaFuncAttributes attr;
+  if (cudaFuncGetAttributes(&attr, vf::vf_batch_end_kernel) != cudaSuccess ||
+      cudaFuncGetAttributes(&attr, vf::vf_batch_advance_kernel) != cudaSuccess)
+    return err(VF_ERR_CUDA, "vf_batch_blocks: loading the batch kernels failed");
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vf::vf_batch_sample_kernel, VF_THREADS, smem);
+  if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  *blocks = (per_sm > 0 ? per_sm : 1) * sms;
+  if (smem_bytes) *smem_bytes = smem;
+  return VF_OK;
+}
+
+int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long long* tile_start,
+                    const int* tile_count, const long long* tile_row, int n_tiles, int max_dim, int* queue,
+                    const unsigned int* call, const double* grids, const double* params, double* partials,
+                    unsigned long long seed, int* flags, int blocks, void* stream) {
+  if (!items || !tile_item || !tile_start || !tile_count || !tile_row || !queue || !call || !grids ||
+      !params || !partials || n_tiles < 0 || blocks < 1)
+    return err(VF_ERR_ARG, "vf_batch_sample: NULL buffer or bad sizes");
+  if (max_dim < 1 || max_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_batch_sample: max_dim must be 1..16");
+  vf::BatchArgs a;
+  a.items = reinterpret_cast<const vf::BatchItem*>(items);
+  a.tile_item = tile_item;
+  a.tile_start = tile_start;
+  a.tile_count = tile_count;
+  a.tile_row = tile_row;
+  a.queue = queue;
+  a.call = call;
+  a.grids = grids;
+  a.params = params;
+  a.partials = partials;
+  a.flags = flags;
+  a.n_tiles = n_tiles;
+  a.max_dim = max_dim;
+  unsigned int k0 = (unsigned int)seed, k1 = (unsigned int)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    a.rk.k0[r] = k0;
+    a.rk.k1[r] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  const int smem = vf::batch_smem_bytes(max_dim);
+  const cudaError_t e = set_smem(smem);
+  if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
+  vf::vf_batch_sample_kernel<<<blocks, VF_THREADS, smem, (cudaStream_t)stream>>>(a);
+  return launched("vf_batch_sample");
+}
+
+int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, const int* blk_role, int n_blocks,
+                           const long long* tile_row, const double* partials, double* grids, double* history,
+                           double* avg, int hist_cap, const int* iter, int* flags, void* stream) {
+  if (!items || !blk_item || !blk_role || !tile_row || !partials || !grids || !history || !avg || !iter ||
+      n_blocks < 1 || hist_cap < 1)
+    return err(VF_ERR_ARG, "vf_batch_iteration_end: NULL buffer or bad sizes");
+  vf::BatchEndArgs a;
+  a.items = reinterpret_cast<const vf::BatchItem*>(items);
+  a.blk_item = blk_item;
+  a.blk_role = blk_role;
+  a.tile_row = tile_row;
+  a.partials = partials;
+  a.grids = grids;
+  a.history = history;
+  a.avg = avg;
+  a.iter = iter;
+  a.flags = flags;
+  a.alpha = 1.5;
+  a.hist_cap = hist_cap;
+  vf::vf_batch_end_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(a);
+  return launched("vf_batch_iteration_end");
+}
+
+int vf_batch_advance(unsigned int* call, int* iter, int* queue, void* stream) {
+  if (!call || !iter || !queue) return err(VF_ERR_ARG, "vf_batch_advance: NULL counter");
+  vf::vf_batch_advance_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(call, iter, queue);
+  return launched("vf_batch_advance");
+}
+
+}  // extern "C"

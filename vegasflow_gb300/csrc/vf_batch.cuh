@@ -1,0 +1,324 @@
+// Batched VEGAS: many independent integrals (own dimension count, event count,
+// integrand, grid) in one persistent fp32 launch per iteration.
+//
+// Work unit: a tile = a contiguous range of at most `tile_events` events of one
+// integral, tile boundaries at fixed multiples within the integral.  A tile's
+// result depends only on the integral and the tile (Philox counter = event index
+// within the integral, stream id = the integral's own id), never on which block
+// ran it or on the other integrals of the batch: an integral gives the same
+// result alone and in any mix (up to the histogram's float atomics order).
+//
+// The sampler is persistent: each block takes tiles from a device queue (an
+// atomic counter), stages the tile's integral (per-bin table, constants) in
+// shared memory when it differs from the previous tile, processes the tile with
+// the same specialised code as the single-integral fp32 kernel, and writes the
+// tile's partial row [res, res2, hist[D][50]] (float64).  The batched
+// iteration-end kernel then sums each integral's tile rows in tile order.
+#pragma once
+#include "vf_refine.cuh"
+#include "vf_vegas_f32.cuh"
+
+namespace vf {
+
+// One integral of a batch (mirrors vf_batch_item in include/vegasflow_gb300.h).
+struct BatchItem {
+  long long n_events;
+  long long grid_off;   // doubles into `grids` ([n_dim][51])
+  long long param_off;  // doubles into `params`
+  double xjac;          // 1 / n_events
+  int n_dim;
+  int integrand;        // VF_INT_SYMGAUSS | VF_INT_GAUSS | VF_INT_BREIT_WIGNER | VF_INT_PROD | VF_INT_SUM
+  int stream_id;        // Philox counter word 3: independent stream per integral
+  int tile0;            // first tile
+  int n_tiles;
+  int train;
+};
+
+struct BatchArgs {
+  const BatchItem* items;
+  const int* tile_item;        // [n_tiles]
+  const long long* tile_start; // [n_tiles] first event of the tile within its integral
+  const int* tile_count;       // [n_tiles]
+  const long long* tile_row;   // [n_tiles] offset (doubles) of the tile's partial row
+  int* queue;                  // work counter, zero at launch
+  const unsigned int* call;    // device: Philox call counter of this iteration
+  const double* grids;
+  const double* params;
+  double* partials;
+  int* flags;
+  int n_tiles;
+  int max_dim;
+  RoundKeys rk;
+};
+
+__host__ __device__ inline int batch_smem_bytes(int max_dim) {
+  return max_dim * VF_BINS * 8 + vegas_f32_joint_floats(max_dim) * 4;
+}
+
+// Stage one integral (table cells, weight constant) in shared memory.
+template <int D, bool GAUSS>
+__device__ __forceinline__ double batch_stage(const BatchItem& it, const double* __restrict__ grids,
+                                              const double* __restrict__ params, float2* cells,
+                                              double* g_mu, double* g_k) {
+  constexpr double SQRT_LOG2E = 1.2011224087864498;
+  const double* grid = grids + it.grid_off;
+  const double* p = params + it.param_off;
+  const int tid = threadIdx.x;
+  if (GAUSS && tid < D) {
+    g_mu[tid] = it.integrand == VF_INT_SYMGAUSS ? 0.5 : p[tid];
+    g_k[tid] = SQRT_LOG2E / (it.integrand == VF_INT_SYMGAUSS ? p[0] : p[D + tid]);
+  }
+  __syncthreads();
+  for (int k = tid; k < D * VF_BINS; k += blockDim.x) {
+    const int d = k / VF_BINS, b = k - d * VF_BINS;
+    const double lo = grid[d * VF_EDGES + b];
+    const double dl = grid[d * VF_EDGES + b + 1] - lo;
+    double c0 = lo - dl, c1 = dl;
+    if (GAUSS) {
+      c0 = (c0 - g_mu[d]) * g_k[d];
+      c1 = c1 * g_k[d];
+    }
+    cells[k] = make_float2((float)c0, (float)c1);
+  }
+  double ws = it.xjac;
+  for (int d = 0; d < D; ++d) ws *= 50.0;
+  if (GAUSS) {
+    double prodk = 1.0;
+    for (int d = 0; d < D; ++d) prodk *= g_k[d];
+    ws *= (it.integrand == VF_INT_SYMGAUSS ? p[1] : 1.0) / prodk;
+  }
+  return ws;
+}
+
+// Process one tile of an integral with D dimensions.
+template <int D, bool GAUSS>
+__device__ void batch_tile(const BatchArgs& a, const BatchItem& it, int tile, bool restage,
+                           unsigned char* smem, double* g_mu, double* g_k, double* s_wscale) {
+  constexpr int NB = D * VF_BINS;
+  constexpr int NP = D / 2;
+  float2* cells = reinterpret_cast<float2*>(smem);
+  float* hist = reinterpret_cast<float*>(smem + a.max_dim * VF_BINS * 8);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool train = it.train != 0;
+  if (restage) {
+    const double ws = batch_stage<D, GAUSS>(it, a.grids, a.params, cells, g_mu, g_k);
+    if (tid == 0) *s_wscale = ws;
+  }
+  if (train)
+    for (int k = tid; k < NP * 2500 + (D & 1) * VF_BINS; k += blockDim.x) hist[k] = 0.0f;
+  __syncthreads();
+  const double wscale = *s_wscale;
+  IntegrandConsts<float, D> kc;
+  if (!GAUSS) load_consts<D>(kc, it.integrand, a.params + it.param_off, D);
+  const u32 call = *a.call;
+  const u32 c3 = (u32)it.stream_id;
+  F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
+  const long long start = a.tile_start[tile];
+  const int count = a.tile_count[tile];
+  for (int j = tid; j < count; j += blockDim.x) {
+    const u64 ev = (u64)(start + j);
+    int bins[D];
+    float x[D];
+    float wf = 1.0f, s = 0.0f;
+#pragma unroll
+    for (int q = 0; q < (D + 3) / 4; ++q) {
+      u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = (call << 4) | (u32)q, cc3 = c3;
+      philox4x32_10_rk(c0, c1, c2, cc3, a.rk);
+      const u32 wq[4] = {c0, c1, c2, cc3};
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) {
+        const int d = 4 * q + jj;
+        if (d < D) {
+          const u64 pp = (u64)(~wq[jj]) * 50ull + 25ull;
+          const int i = (int)(pp >> 32);
+          const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
+          const float2 c = cells[d * VF_BINS + i];
+          const float t = fmaf(c.y, m, c.x);
+          wf = (d == 0) ? c.y : wf * c.y;
+          if (GAUSS)
+            s = fmaf(t, t, s);
+          else
+            x[d] = t;
+          bins[d] = i;
+        }
+      }
+    }
+    const float f = GAUSS ? ex2_approx_ftz(-s) : eval_builtin<D>(it.integrand, x, D, kc);
+    const float v = wf * f;
+    const float v2 = v * v;
+    two_sum_add(s1, v);
+    two_sum_add(s2, v2);
+    if (train) {
+#pragma unroll
+      for (int pq = 0; pq < NP; ++pq) atomicAdd(hist + pq * 2500 + bins[2 * pq] * VF_BINS + bins[2 * pq + 1], v2);
+      if (D & 1) atomicAdd(hist + NP * 2500 + bins[D - 1], v2);
+    }
+  }
+  __shared__ double red[2][VF_THREADS / 32];
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  if (lane == 0) {
+    red[0][warp] = (double)s1.s + (double)s1.c;
+    red[1][warp] = (double)s2.s + (double)s2.c;
+  }
+  __syncthreads();
+  double* row = a.partials + a.tile_row[tile];
+  if (tid == 0) {
+    double b1 = 0.0, b2 = 0.0;
+    for (int i = 0; i < VF_THREADS / 32; ++i) {
+      b1 += red[0][i];
+      b2 += red[1][i];
+    }
+    row[0] = b1 * wscale;
+    row[1] = b2 * wscale * wscale;
+  }
+  if (train) {
+    const double s2c = wscale * wscale;
+    for (int k = tid; k < NB; k += blockDim.x) {
+      const int d = k / VF_BINS, b = k - d * VF_BINS;
+      float hf = 0.0f;
+      if (d < 2 * NP) {
+        const float* tab = hist + (d >> 1) * 2500;
+        if ((d & 1) == 0)
+          for (int c = 0; c < VF_BINS; ++c) hf += tab[b * VF_BINS + c];
+        else
+          for (int r = 0; r < VF_BINS; ++r) hf += tab[r * VF_BINS + b];
+      } else {
+        hf = hist[NP * 2500 + b];
+      }
+      row[2 + k] = (double)hf * s2c;
+    }
+  }
+  __syncthreads();  // the shared tables are reused by the next tile
+}
+
+template <bool GAUSS>
+__device__ __forceinline__ void batch_dispatch(int D, const BatchArgs& a, const BatchItem& it, int tile,
+                                               bool restage, unsigned char* smem, double* g_mu,
+                                               double* g_k, double* s_ws) {
+  switch (D) {
+#define VF_BATCH_CASE(n) \
+  case n: batch_tile<n, GAUSS>(a, it, tile, restage, smem, g_mu, g_k, s_ws); break;
+    VF_BATCH_CASE(1) VF_BATCH_CASE(2) VF_BATCH_CASE(3) VF_BATCH_CASE(4) VF_BATCH_CASE(5)
+    VF_BATCH_CASE(6) VF_BATCH_CASE(7) VF_BATCH_CASE(8) VF_BATCH_CASE(9) VF_BATCH_CASE(10)
+    VF_BATCH_CASE(11) VF_BATCH_CASE(12) VF_BATCH_CASE(13) VF_BATCH_CASE(14) VF_BATCH_CASE(15)
+    VF_BATCH_CASE(16)
+#undef VF_BATCH_CASE
+    default: break;
+  }
+}
+
+__global__ void __launch_bounds__(VF_THREADS, 2) vf_batch_sample_kernel(const BatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double g_mu[VF_MAX_DIM], g_k[VF_MAX_DIM], s_ws;
+  __shared__ int s_tile;
+  int cur_item = -1;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(a.queue, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    __syncthreads();
+    if (tile >= a.n_tiles) break;
+    const int item = a.tile_item[tile];
+    const BatchItem it = a.items[item];
+    const bool restage = item != cur_item;
+    cur_item = item;
+    if (it.integrand == VF_INT_SYMGAUSS || it.integrand == VF_INT_GAUSS)
+      batch_dispatch<true>(it.n_dim, a, it, tile, restage, smem, g_mu, g_k, &s_ws);
+    else
+      batch_dispatch<false>(it.n_dim, a, it, tile, restage, smem, g_mu, g_k, &s_ws);
+  }
+}
+
+// Batched iteration end: block b serves (item blk_item[b], role blk_role[b]);
+// role d >= 0 sums histogram column d over the item's tiles and refines that
+// grid row; role -1 sums res/res2, sigma, history and the weighted average.
+struct BatchEndArgs {
+  const BatchItem* items;
+  const int* blk_item;
+  const int* blk_role;
+  const long long* tile_row;
+  const double* partials;
+  double* grids;
+  double* history;          // [n_items][hist_cap][2]
+  double* avg;              // [n_items][5]
+  const int* iter;          // device iteration index (history slot)
+  int* flags;
+  double alpha;
+  int hist_cap;
+};
+
+__global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a) {
+  const int t = threadIdx.x;
+  const int item = a.blk_item[blockIdx.x];
+  const int role = a.blk_role[blockIdx.x];
+  const BatchItem it = a.items[item];
+  __shared__ double part[4][64];
+  __shared__ double hsm[VF_BINS];
+  __shared__ double red[2][256];
+  if (role >= 0) {
+    if (!it.train) return;
+    const int c = t & 63, r0 = t >> 6;
+    double s = 0.0;
+    if (c < VF_BINS)
+      for (int k = r0; k < it.n_tiles; k += 4) s += a.partials[a.tile_row[it.tile0 + k] + 2 + role * VF_BINS + c];
+    part[r0][c] = s;
+    __syncthreads();
+    if (t < VF_BINS) hsm[t] = ((part[0][t] + part[1][t]) + part[2][t]) + part[3][t];
+    __syncthreads();
+    refine_dimension(hsm, a.grids + it.grid_off + role * VF_EDGES, a.alpha, a.flags);
+    return;
+  }
+  double s1 = 0.0, s2 = 0.0;
+  for (int k = t; k < it.n_tiles; k += blockDim.x) {
+    const double* row = a.partials + a.tile_row[it.tile0 + k];
+    s1 += row[0];
+    s2 += row[1];
+  }
+  red[0][t] = s1;
+  red[1][t] = s2;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (t < o) {
+      red[0][t] += red[0][t + o];
+      red[1][t] += red[1][t + o];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    const int iter = *a.iter;
+    const double res = red[0][0], res2 = red[1][0];
+    const double N = (double)it.n_events;
+    const double err = __ddiv_rn(__dsub_rn(__dmul_rn(N, res2), __dmul_rn(res, res)), __dsub_rn(N, 1.0));
+    const double sigma = sqrt(fmax(err, 0.0));
+    double* h = a.history + ((long long)item * a.hist_cap + (iter < a.hist_cap ? iter : a.hist_cap - 1)) * 2;
+    h[0] = res;
+    h[1] = sigma;
+    double* av = a.avg + 5LL * item;
+    const double wgt = 1.0 / __dmul_rn(sigma, sigma);
+    av[0] = __dadd_rn(av[0], __dmul_rn(res, wgt));
+    av[1] = __dadd_rn(av[1], wgt);
+    const double mean = av[0] / av[1];
+    av[2] = mean;
+    av[3] = sqrt(1.0 / av[1]);
+    double chi2 = 0.0;
+    const int last = iter < a.hist_cap ? iter : a.hist_cap - 1;
+    for (int i = 0; i <= last; ++i) {
+      const double* hi = a.history + ((long long)item * a.hist_cap + i) * 2;
+      chi2 += (hi[0] - mean) * (hi[0] - mean) / (hi[1] * hi[1]);
+    }
+    av[4] = last > 0 ? chi2 / last : 0.0;
+    if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+  }
+}
+
+// Advance the per-iteration device counters and re-arm the work queue.
+__global__ void vf_batch_advance_kernel(unsigned int* call, int* iter, int* queue) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    *call += 1u;
+    *iter += 1;
+    *queue = 0;
+  }
+}
+
+}  // namespace vf
