@@ -172,10 +172,13 @@ int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, lo
  * is split into tiles of at most T events (fixed boundaries within the
  * integral); tile k's partial row [res, res2, hist[n_dim][50]] lives at
  * partials + tile_row[k].  The Philox stream of an integral is keyed by the
- * batch seed with its own stream_id, so its result does not depend on the
- * batch.  The per-iteration counters (call, iter, queue) live on the device:
- * an iteration is sample -> iteration_end -> advance, all capturable in a
- * CUDA graph.
+ * batch seed with its own stream_id and its own call counter, so its result
+ * does not depend on the batch.  Per-integral state lives in slots:
+ * iters[slot] (iterations in the running average), calls[slot] (Philox call
+ * counter), history[slot][hist_cap][2], avg[slot][5]; integrals can join and
+ * leave between iterations.  An iteration is vf_batch_sample followed by
+ * vf_batch_iteration_end (which advances the counters and re-arms the queue),
+ * so it can be captured in a CUDA graph.
  */
 typedef struct vf_batch_item {
   long long n_events;
@@ -188,23 +191,25 @@ typedef struct vf_batch_item {
   int tile0;            /* first tile of this integral */
   int n_tiles;
   int train;
+  int slot;             /* state slot */
+  int pad;
 } vf_batch_item;
 
 /* Persistent grid size and dynamic shared memory for a batch whose largest n_dim is max_dim. */
 int vf_batch_blocks(int max_dim, int* blocks, int* smem_bytes);
-/* One iteration's events of every integral; *queue must be 0 (vf_batch_advance re-arms it). */
+/* One iteration's events of every integral; *queue must be 0 (vf_batch_iteration_end re-arms it). */
 int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long long* tile_start,
                     const int* tile_count, const long long* tile_row, int n_tiles, int max_dim, int* queue,
-                    const unsigned int* call, const double* grids, const double* params, double* partials,
+                    const unsigned int* calls, const double* grids, const double* params, double* partials,
                     unsigned long long seed, int* flags, int blocks, void* stream);
-/* Per integral: sums of its tile rows in tile order, sigma, history[item][*iter], the
- * weighted average avg[item][5]; per (integral, dimension) block: refinement.  Block b
- * serves integral blk_item[b] in role blk_role[b] (a dimension, or -1 for the sums). */
+/* Per integral: sums of its tile rows in tile order, sigma, history[slot][iters[slot]],
+ * the weighted average avg[slot][5], then iters[slot] += 1, calls[slot] += 1; per
+ * (integral, dimension) block: refinement of that grid row; *queue = 0.  Block b serves
+ * integral blk_item[b] in role blk_role[b] (a dimension, or -1 for the sums). */
 int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, const int* blk_role, int n_blocks,
                            const long long* tile_row, const double* partials, double* grids, double* history,
-                           double* avg, int hist_cap, const int* iter, int* flags, void* stream);
-/* *call += 1, *iter += 1, *queue = 0 (on the stream). */
-int vf_batch_advance(unsigned int* call, int* iter, int* queue, void* stream);
+                           double* avg, int hist_cap, int* iters, unsigned int* calls, int* queue, int* flags,
+                           void* stream);
 
 /* VegasFlow.refine_grid(arr_res2) (vflow.py:349-362): hist [n_dim][50]. */
 int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, int* flags,

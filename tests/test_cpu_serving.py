@@ -1,0 +1,55 @@
+"""Host-side logic of the serving loop and the batch engine (no GPU)."""
+
+import numpy as np
+
+from vegasflow_gb300 import integrands
+from vegasflow_gb300.batch import ITEM_DTYPE, c4_specs
+from vegasflow_gb300.serving import percentile, poisson_workload, request_footprint, step_tables
+
+
+def test_step_tables_cover_every_event():
+    n_events = [10, 65536, 65537, 300_000, 1]
+    n_dim = [2, 8, 16, 3, 1]
+    t = step_tables(n_events, n_dim, slots=[4, 0, 7, 2, 9], stream_ids=[1, 2, 3, 4, 5],
+                    integrand_ids=[1, 2, 2, 3, 4], grid_off=[0, 1, 2, 3, 4], param_off=[0, 1, 2, 3, 4],
+                    tile_events=65536)
+    items = t["items"]
+    assert items.dtype == ITEM_DTYPE and list(items["slot"]) == [4, 0, 7, 2, 9]
+    for i, (n, d) in enumerate(zip(n_events, n_dim)):
+        sel = t["tile_item"] == i
+        assert items["n_tiles"][i] == sel.sum() == -(-n // 65536)
+        assert items["tile0"][i] == np.flatnonzero(sel)[0]
+        assert t["tile_count"][sel].sum() == n
+        np.testing.assert_array_equal(t["tile_start"][sel], np.arange(sel.sum()) * 65536)
+        # iteration-end blocks: one per dimension and one for the sums
+        roles = t["blk_role"][t["blk_item"] == i]
+        np.testing.assert_array_equal(roles, list(range(d)) + [-1])
+    widths = 2 + 50 * np.repeat(n_dim, items["n_tiles"])
+    np.testing.assert_array_equal(np.diff(t["tile_row"]), widths[:-1])
+    assert t["rows_total"] == widths.sum()
+
+
+def test_footprint_grows_with_tiles():
+    a = request_footprint(8, 10_000)
+    b = request_footprint(8, 10_000_000)
+    assert 0 < a < b and b < 1e8
+
+
+def test_poisson_workload_statistics():
+    reqs = poisson_workload(rate=200.0, duration=60.0, seed=9)
+    assert 11_000 < len(reqs) < 13_000
+    arr = np.array([r.arrival for r in reqs])
+    assert np.all(np.diff(arr) > 0) and arr[-1] <= 60.0
+    bw = np.mean([r.integrand.__name__ == "breit_wigner" for r in reqs])
+    assert 0.17 < bw < 0.23
+    dims = [r.n_dim for r in reqs if r.integrand.__name__ == "gauss"]
+    assert min(dims) == 2 and max(dims) == 16
+    assert all(r.target_rel_sigma == 1e-3 and r.max_iterations == 20 for r in reqs)
+
+
+def test_percentile_and_c4_specs():
+    assert percentile([1, 2, 3, 4], 50) == 2.5
+    specs = c4_specs()
+    assert len(specs) == 1024
+    assert all(2 <= d <= 16 and 10_000 <= n <= 10_000_000 for d, n, _ in specs)
+    assert all(isinstance(f, integrands.DeviceIntegrand) for _, _, f in specs)

@@ -71,8 +71,7 @@ SIGNATURES = {
                               _P, _I, _P, _P],
     "vf_batch_blocks": [_I, _P, _P],
     "vf_batch_sample": [_P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],
-    "vf_batch_iteration_end": [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P],
-    "vf_batch_advance": [_P, _P, _P, _P],
+    "vf_batch_iteration_end": [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P],
     "vf_tune_set": [_I, _I],
     "vf_tune_get": [_I, _P],
 }

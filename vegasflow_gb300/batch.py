@@ -2,11 +2,11 @@
 
 ``VegasBatch`` integrates a list of (n_dim, n_events, device integrand) with
 their own grids, all in fp32 fused form: per iteration one persistent sampler
-launch over a device work queue of fixed-size event tiles, one batched
+launch over a device work queue of fixed-size event tiles and one batched
 iteration-end launch (sums, sigma, weighted average, refinement of every grid
-row) and one counter-advance launch.  The three launches can be captured once
-in a CUDA graph and replayed (``graph=True``); every per-iteration quantity
-(Philox call counter, history slot, queue) lives on the device.
+row, counter advance).  The two launches can be captured once in a CUDA graph
+and replayed (``graph=True``); every per-iteration quantity (Philox call
+counters, history slots, the work queue) lives on the device.
 
 An integral's result depends only on itself (its own Philox stream id, fixed
 tile boundaries): the same integral alone and in any mix agrees to the
@@ -27,8 +27,8 @@ from .integrands import DeviceIntegrand
 
 ITEM_DTYPE = np.dtype([("n_events", "<i8"), ("grid_off", "<i8"), ("param_off", "<i8"), ("xjac", "<f8"),
                        ("n_dim", "<i4"), ("integrand", "<i4"), ("stream_id", "<i4"), ("tile0", "<i4"),
-                       ("n_tiles", "<i4"), ("train", "<i4")])
-assert ITEM_DTYPE.itemsize == 56
+                       ("n_tiles", "<i4"), ("train", "<i4"), ("slot", "<i4"), ("pad", "<i4")])
+assert ITEM_DTYPE.itemsize == 64
 
 DEFAULT_TILE_EVENTS = 1 << 16
 
@@ -73,7 +73,7 @@ class VegasBatch:
             n_tiles = (n_events + self.tile_events - 1) // self.tile_events
             width = 2 + BINS_MAX * n_dim
             items[i] = (n_events, goff, poff, 1.0 / n_events, n_dim, integ.integrand_id, stream_ids[i],
-                        len(tile_item), n_tiles, int(bool(train)))
+                        len(tile_item), n_tiles, int(bool(train)), i, 0)
             for k in range(n_tiles):
                 tile_item.append(i)
                 tile_start.append(k * self.tile_events)
@@ -105,8 +105,8 @@ class VegasBatch:
         self.partials = torch.zeros(max(roff, 1), dtype=torch.float64, device=dev)
         self.history = torch.zeros((self.n_items, self.hist_cap, 2), dtype=torch.float64, device=dev)
         self.avg = torch.zeros((self.n_items, 5), dtype=torch.float64, device=dev)
-        self._call = torch.zeros(1, dtype=torch.int32, device=dev)
-        self._iter = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._calls = torch.zeros(self.n_items, dtype=torch.int32, device=dev)
+        self._iters = torch.zeros(self.n_items, dtype=torch.int32, device=dev)
         self._queue = torch.zeros(1, dtype=torch.int32, device=dev)
         self._flags = torch.zeros(1, dtype=torch.int32, device=dev)
         blocks, smem = ctypes.c_int(0), ctypes.c_int(0)
@@ -121,25 +121,25 @@ class VegasBatch:
         s = nat.stream_handle()
         nat.check(lib.vf_batch_sample(nat.ptr(self._items), nat.ptr(self._tile_item), nat.ptr(self._tile_start),
                                       nat.ptr(self._tile_count), nat.ptr(self._tile_row), self.n_tiles,
-                                      self.max_dim, nat.ptr(self._queue), nat.ptr(self._call),
+                                      self.max_dim, nat.ptr(self._queue), nat.ptr(self._calls),
                                       nat.ptr(self.grids), nat.ptr(self.params), nat.ptr(self.partials),
                                       self.seed, nat.ptr(self._flags), self.blocks, s))
         nat.check(lib.vf_batch_iteration_end(nat.ptr(self._items), nat.ptr(self._blk_item),
                                              nat.ptr(self._blk_role), int(self._blk_item.numel()),
                                              nat.ptr(self._tile_row), nat.ptr(self.partials),
                                              nat.ptr(self.grids), nat.ptr(self.history), nat.ptr(self.avg),
-                                             self.hist_cap, nat.ptr(self._iter), nat.ptr(self._flags), s))
-        nat.check(lib.vf_batch_advance(nat.ptr(self._call), nat.ptr(self._iter), nat.ptr(self._queue), s))
+                                             self.hist_cap, nat.ptr(self._iters), nat.ptr(self._calls),
+                                             nat.ptr(self._queue), nat.ptr(self._flags), s))
 
     def reset_average(self):
         """Start a new weighted average (history slots restart at 0); the grids
         and the Philox call counter carry on."""
         self.avg.zero_()
-        self._iter.zero_()
+        self._iters.zero_()
         self.iterations_done = 0
 
     def capture(self):
-        """Capture one iteration (3 launches) in a CUDA graph."""
+        """Capture one iteration (2 launches) in a CUDA graph."""
         torch.cuda.synchronize(self.device)
         side = torch.cuda.Stream(device=self.device)
         side.wait_stream(torch.cuda.current_stream(self.device))

@@ -47,8 +47,9 @@ int vf_batch_blocks(int max_dim, int* blocks, int* smem_bytes) {
   // load the batch kernels now, so that a later stream capture launches only
   cudaFuncAttributes attr;
   if (cudaFuncGetAttributes(&attr, vf::vf_batch_end_kernel) != cudaSuccess ||
-      cudaFuncGetAttributes(&attr, vf::vf_batch_advance_kernel) != cudaSuccess)
+      cudaFuncGetAttributes(&attr, vf::vf_batch_sample_kernel) != cudaSuccess)
     return err(VF_ERR_CUDA, "vf_batch_blocks: loading the batch kernels failed");
+  (void)attr;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vf::vf_batch_sample_kernel, VF_THREADS, smem);
   if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
@@ -62,9 +63,9 @@ int vf_batch_blocks(int max_dim, int* blocks, int* smem_bytes) {
 
 int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long long* tile_start,
                     const int* tile_count, const long long* tile_row, int n_tiles, int max_dim, int* queue,
-                    const unsigned int* call, const double* grids, const double* params, double* partials,
+                    const unsigned int* calls, const double* grids, const double* params, double* partials,
                     unsigned long long seed, int* flags, int blocks, void* stream) {
-  if (!items || !tile_item || !tile_start || !tile_count || !tile_row || !queue || !call || !grids ||
+  if (!items || !tile_item || !tile_start || !tile_count || !tile_row || !queue || !calls || !grids ||
       !params || !partials || n_tiles < 0 || blocks < 1)
     return err(VF_ERR_ARG, "vf_batch_sample: NULL buffer or bad sizes");
   if (max_dim < 1 || max_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_batch_sample: max_dim must be 1..16");
@@ -75,7 +76,7 @@ int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long
   a.tile_count = tile_count;
   a.tile_row = tile_row;
   a.queue = queue;
-  a.call = call;
+  a.calls = calls;
   a.grids = grids;
   a.params = params;
   a.partials = partials;
@@ -98,8 +99,10 @@ int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long
 
 int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, const int* blk_role, int n_blocks,
                            const long long* tile_row, const double* partials, double* grids, double* history,
-                           double* avg, int hist_cap, const int* iter, int* flags, void* stream) {
-  if (!items || !blk_item || !blk_role || !tile_row || !partials || !grids || !history || !avg || !iter ||
+                           double* avg, int hist_cap, int* iters, unsigned int* calls, int* queue, int* flags,
+                           void* stream) {
+  if (!items || !blk_item || !blk_role || !tile_row || !partials || !grids || !history || !avg || !iters ||
+      !calls || !queue ||
       n_blocks < 1 || hist_cap < 1)
     return err(VF_ERR_ARG, "vf_batch_iteration_end: NULL buffer or bad sizes");
   vf::BatchEndArgs a;
@@ -111,18 +114,14 @@ int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, cons
   a.grids = grids;
   a.history = history;
   a.avg = avg;
-  a.iter = iter;
+  a.iters = iters;
+  a.calls = calls;
+  a.queue = queue;
   a.flags = flags;
   a.alpha = 1.5;
   a.hist_cap = hist_cap;
   vf::vf_batch_end_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(a);
   return launched("vf_batch_iteration_end");
-}
-
-int vf_batch_advance(unsigned int* call, int* iter, int* queue, void* stream) {
-  if (!call || !iter || !queue) return err(VF_ERR_ARG, "vf_batch_advance: NULL counter");
-  vf::vf_batch_advance_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(call, iter, queue);
-  return launched("vf_batch_advance");
 }
 
 }  // extern "C"

@@ -8,6 +8,10 @@
 // ran it or on the other integrals of the batch: an integral gives the same
 // result alone and in any mix (up to the histogram's float atomics order).
 //
+// Per-integral state lives in slots (iteration index, Philox call counter,
+// history, running average), so integrals can join and leave a batch between
+// iterations (continuous batching) while keeping their own progress.
+//
 // The sampler is persistent: each block takes tiles from a device queue (an
 // atomic counter), stages the tile's integral (per-bin table, constants) in
 // shared memory when it differs from the previous tile, processes the tile with
@@ -32,6 +36,8 @@ struct BatchItem {
   int tile0;            // first tile
   int n_tiles;
   int train;
+  int slot;             // state slot: iters[slot], calls[slot], history[slot], avg[slot]
+  int pad;
 };
 
 struct BatchArgs {
@@ -41,7 +47,7 @@ struct BatchArgs {
   const int* tile_count;       // [n_tiles]
   const long long* tile_row;   // [n_tiles] offset (doubles) of the tile's partial row
   int* queue;                  // work counter, zero at launch
-  const unsigned int* call;    // device: Philox call counter of this iteration
+  const unsigned int* calls;   // [slots] Philox call counter of each integral's iteration
   const double* grids;
   const double* params;
   double* partials;
@@ -110,7 +116,7 @@ __device__ void batch_tile(const BatchArgs& a, const BatchItem& it, int tile, bo
   const double wscale = *s_wscale;
   IntegrandConsts<float, D> kc;
   if (!GAUSS) load_consts<D>(kc, it.integrand, a.params + it.param_off, D);
-  const u32 call = *a.call;
+  const u32 call = a.calls[it.slot];
   const u32 c3 = (u32)it.stream_id;
   F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
   const long long start = a.tile_start[tile];
@@ -232,7 +238,9 @@ __global__ void __launch_bounds__(VF_THREADS, 2) vf_batch_sample_kernel(const Ba
 
 // Batched iteration end: block b serves (item blk_item[b], role blk_role[b]);
 // role d >= 0 sums histogram column d over the item's tiles and refines that
-// grid row; role -1 sums res/res2, sigma, history and the weighted average.
+// grid row; role -1 sums res/res2, sigma, history and the weighted average of
+// the item's slot, then advances the slot's counters.  Block 0 re-arms the
+// sampler's work queue (the sampler launch has completed: stream order).
 struct BatchEndArgs {
   const BatchItem* items;
   const int* blk_item;
@@ -240,9 +248,11 @@ struct BatchEndArgs {
   const long long* tile_row;
   const double* partials;
   double* grids;
-  double* history;          // [n_items][hist_cap][2]
-  double* avg;              // [n_items][5]
-  const int* iter;          // device iteration index (history slot)
+  double* history;          // [slots][hist_cap][2]
+  double* avg;              // [slots][5]
+  int* iters;               // [slots] iterations in the current average (history index)
+  unsigned int* calls;      // [slots] Philox call counters
+  int* queue;               // the sampler's work counter, re-armed here
   int* flags;
   double alpha;
   int hist_cap;
@@ -286,15 +296,17 @@ __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a)
     __syncthreads();
   }
   if (t == 0) {
-    const int iter = *a.iter;
+    const int slot = it.slot;
+    const int iter = a.iters[slot];
+    const int hs = iter < a.hist_cap ? iter : a.hist_cap - 1;
     const double res = red[0][0], res2 = red[1][0];
     const double N = (double)it.n_events;
     const double err = __ddiv_rn(__dsub_rn(__dmul_rn(N, res2), __dmul_rn(res, res)), __dsub_rn(N, 1.0));
     const double sigma = sqrt(fmax(err, 0.0));
-    double* h = a.history + ((long long)item * a.hist_cap + (iter < a.hist_cap ? iter : a.hist_cap - 1)) * 2;
+    double* h = a.history + ((long long)slot * a.hist_cap + hs) * 2;
     h[0] = res;
     h[1] = sigma;
-    double* av = a.avg + 5LL * item;
+    double* av = a.avg + 5LL * slot;
     const double wgt = 1.0 / __dmul_rn(sigma, sigma);
     av[0] = __dadd_rn(av[0], __dmul_rn(res, wgt));
     av[1] = __dadd_rn(av[1], wgt);
@@ -302,22 +314,15 @@ __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a)
     av[2] = mean;
     av[3] = sqrt(1.0 / av[1]);
     double chi2 = 0.0;
-    const int last = iter < a.hist_cap ? iter : a.hist_cap - 1;
-    for (int i = 0; i <= last; ++i) {
-      const double* hi = a.history + ((long long)item * a.hist_cap + i) * 2;
+    for (int i = 0; i <= hs; ++i) {
+      const double* hi = a.history + ((long long)slot * a.hist_cap + i) * 2;
       chi2 += (hi[0] - mean) * (hi[0] - mean) / (hi[1] * hi[1]);
     }
-    av[4] = last > 0 ? chi2 / last : 0.0;
+    av[4] = hs > 0 ? chi2 / hs : 0.0;
     if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
-  }
-}
-
-// Advance the per-iteration device counters and re-arm the work queue.
-__global__ void vf_batch_advance_kernel(unsigned int* call, int* iter, int* queue) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    *call += 1u;
-    *iter += 1;
-    *queue = 0;
+    a.iters[slot] = iter + 1;
+    a.calls[slot] += 1u;
+    if (blockIdx.x == 0) *a.queue = 0;  // the sampler has finished (stream order)
   }
 }
 

@@ -1,0 +1,323 @@
+"""Continuous-batching integration server.
+
+Requests (an integrand, n_dim, events per iteration, a target relative sigma
+and an iteration cap) arrive over time.  The server keeps every active
+request's grid, running average and counters resident on the GPU in a slot
+pool and advances *all* active requests by one VEGAS iteration per step -- one
+persistent batched sampler launch plus one batched iteration-end launch.
+Between steps it retires the requests that reached their target (or their
+iteration cap) and admits waiting ones while slots and the HBM budget allow,
+so requests that arrive while others are on the GPU join at the next step
+and their work overlaps with everyone else's.
+
+An integral's numbers depend only on itself (its Philox stream id and fixed
+event tiles): a request gives the same result alone and in any mix, up to the
+rounding of the histogram's float atomics.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .batch import DEFAULT_TILE_EVENTS, ITEM_DTYPE
+from .configflow import BINS_MAX
+from .integrands import DeviceIntegrand
+
+MAX_DIM = 16
+PARAMS_PER_SLOT = 2 * MAX_DIM + 2
+
+
+@dataclass
+class Request:
+    n_dim: int
+    n_events: int
+    integrand: DeviceIntegrand
+    target_rel_sigma: float = 1e-3
+    max_iterations: int = 20
+    arrival: float = 0.0
+    rid: int = -1
+    # filled in by the server
+    result: float = float("nan")
+    sigma: float = float("nan")
+    iterations: int = 0
+    converged: bool = False
+    admitted: float = float("nan")
+    finished: float = float("nan")
+    slot: int = -1
+    exact: float = field(default=float("nan"), repr=False)
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+def step_tables(n_events, n_dim, slots, stream_ids, integrand_ids, grid_off, param_off, tile_events, train=True):
+    """The per-step device tables for the active requests (host side, vectorised):
+    items, tiles (item, first event, count, partial-row offset) and the
+    iteration-end block table (item, role)."""
+    n_events = np.asarray(n_events, dtype=np.int64)
+    n_dim = np.asarray(n_dim, dtype=np.int64)
+    n = n_events.size
+    n_tiles = (n_events + tile_events - 1) // tile_events
+    tile0 = np.concatenate([[0], np.cumsum(n_tiles)[:-1]]).astype(np.int64)
+    total = int(n_tiles.sum())
+    tile_item = np.repeat(np.arange(n, dtype=np.int32), n_tiles)
+    k = np.arange(total, dtype=np.int64) - np.repeat(tile0, n_tiles)
+    tile_start = k * tile_events
+    tile_count = np.minimum(tile_events, np.repeat(n_events, n_tiles) - tile_start).astype(np.int32)
+    width = 2 + BINS_MAX * np.repeat(n_dim, n_tiles)
+    tile_row = np.concatenate([[0], np.cumsum(width)[:-1]]).astype(np.int64)
+    rows_total = int(width.sum())
+    items = np.zeros(n, dtype=ITEM_DTYPE)
+    items["n_events"] = n_events
+    items["grid_off"] = grid_off
+    items["param_off"] = param_off
+    items["xjac"] = 1.0 / n_events
+    items["n_dim"] = n_dim
+    items["integrand"] = integrand_ids
+    items["stream_id"] = stream_ids
+    items["tile0"] = tile0
+    items["n_tiles"] = n_tiles
+    items["train"] = int(bool(train))
+    items["slot"] = slots
+    blk_item = np.repeat(np.arange(n, dtype=np.int32), n_dim + 1)
+    starts = np.concatenate([[0], np.cumsum(n_dim + 1)[:-1]])
+    blk_role = (np.arange(int((n_dim + 1).sum())) - np.repeat(starts, n_dim + 1)).astype(np.int32)
+    last = starts + n_dim
+    blk_role[last] = -1
+    return dict(items=items, tile_item=tile_item, tile_start=tile_start, tile_count=tile_count,
+                tile_row=tile_row, blk_item=blk_item, blk_role=blk_role, rows_total=rows_total,
+                n_tiles=total)
+
+
+def request_footprint(n_dim, n_events, tile_events=DEFAULT_TILE_EVENTS, hist_cap=32):
+    """Device bytes a request holds while active: its slot (grid, parameters,
+    history, average, counters) and its partial rows."""
+    n_tiles = (n_events + tile_events - 1) // tile_events
+    rows = n_tiles * (2 + BINS_MAX * n_dim) * 8
+    slot = (MAX_DIM * (BINS_MAX + 1) + PARAMS_PER_SLOT + 2 * hist_cap + 5) * 8 + 8
+    return rows + slot + n_tiles * 24
+
+
+def percentile(values, q):
+    v = np.sort(np.asarray(values, dtype=np.float64))
+    if v.size == 0:
+        return float("nan")
+    return float(np.percentile(v, q))
+
+
+class VegasServer:
+    """Continuous batching over a GPU slot pool.
+
+    ``max_slots`` bounds the number of concurrently active requests;
+    ``hbm_budget`` (bytes) bounds the device memory they hold (admission
+    control); ``seed`` keys every request's Philox stream (with its request id as
+    stream id)."""
+
+    def __init__(self, max_slots=2048, hbm_budget=150e9, tile_events=DEFAULT_TILE_EVENTS, seed=1234,
+                 hist_cap=32, device=None):
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if self.device.type != "cuda":
+            raise RuntimeError("VegasServer runs on a CUDA device only")
+        nat.load()
+        self.max_slots = int(max_slots)
+        self.hbm_budget = float(hbm_budget)
+        self.tile_events = int(tile_events)
+        self.seed = int(seed)
+        self.hist_cap = int(hist_cap)
+        dev = self.device
+        self.grids = torch.zeros(self.max_slots * MAX_DIM * (BINS_MAX + 1), dtype=torch.float64, device=dev)
+        self.params = torch.zeros(self.max_slots * PARAMS_PER_SLOT, dtype=torch.float64, device=dev)
+        self.history = torch.zeros((self.max_slots, self.hist_cap, 2), dtype=torch.float64, device=dev)
+        self.avg = torch.zeros((self.max_slots, 5), dtype=torch.float64, device=dev)
+        self.iters = torch.zeros(self.max_slots, dtype=torch.int32, device=dev)
+        self.calls = torch.zeros(self.max_slots, dtype=torch.int32, device=dev)
+        self._queue = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._flags = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.partials = torch.zeros(1 << 20, dtype=torch.float64, device=dev)
+        blocks, smem = ctypes.c_int(0), ctypes.c_int(0)
+        nat.check(nat.load().vf_batch_blocks(MAX_DIM, ctypes.byref(blocks), ctypes.byref(smem)))
+        self.blocks = blocks.value
+        self._uniform_row = torch.as_tensor(np.linspace(0.0, 1.0, BINS_MAX + 1), dtype=torch.float64, device=dev)
+        self.free_slots = list(range(self.max_slots - 1, -1, -1))
+        self.active = []          # requests on the GPU
+        self.waiting = []         # arrived, not admitted yet
+        self.done = []
+        self.bytes_in_use = 0.0
+        self.events_done = 0
+        self.steps = 0
+        self._next_rid = 0
+
+    # ---------------------------------------------------------------- admission
+    def submit(self, req: Request):
+        if not isinstance(req.integrand, DeviceIntegrand) or not 1 <= req.n_dim <= MAX_DIM:
+            raise ValueError("requests need a built-in DeviceIntegrand and 1 <= n_dim <= 16")
+        if req.rid < 0:
+            req.rid = self._next_rid
+        self._next_rid = max(self._next_rid, req.rid + 1)
+        self.waiting.append(req)
+
+    def _admit(self, now):
+        admitted = []
+        keep = []
+        for req in self.waiting:
+            fp = request_footprint(req.n_dim, req.n_events, self.tile_events, self.hist_cap)
+            if self.free_slots and self.bytes_in_use + fp <= self.hbm_budget:
+                req.slot = self.free_slots.pop()
+                req.admitted = now
+                req._footprint = fp
+                self.bytes_in_use += fp
+                admitted.append(req)
+            else:
+                keep.append(req)
+        self.waiting = keep
+        if not admitted:
+            return
+        slots = torch.as_tensor([r.slot for r in admitted], dtype=torch.int64, device=self.device)
+        grid_rows = self.grids.view(self.max_slots, MAX_DIM, BINS_MAX + 1)
+        grid_rows[slots] = self._uniform_row
+        p = np.zeros((len(admitted), PARAMS_PER_SLOT))
+        for i, r in enumerate(admitted):
+            pr = r.integrand.params(r.n_dim)
+            p[i, : pr.size] = pr
+        self.params.view(self.max_slots, PARAMS_PER_SLOT)[slots] = torch.as_tensor(p, device=self.device)
+        self.history[slots] = 0.0
+        self.avg[slots] = 0.0
+        self.iters[slots] = 0
+        self.calls[slots] = 0
+        self.active.extend(admitted)
+
+    # ---------------------------------------------------------------- one step
+    def step(self, now_fn):
+        """Advance every active request by one iteration, then retire finished ones."""
+        act = self.active
+        t = step_tables([r.n_events for r in act], [r.n_dim for r in act], [r.slot for r in act],
+                        [r.rid for r in act], [r.integrand.integrand_id for r in act],
+                        [r.slot * MAX_DIM * (BINS_MAX + 1) for r in act],
+                        [r.slot * PARAMS_PER_SLOT for r in act], self.tile_events)
+        if t["rows_total"] > self.partials.numel():
+            self.partials = torch.zeros(int(t["rows_total"] * 1.5), dtype=torch.float64, device=self.device)
+        dev = self.device
+        items = torch.from_numpy(t["items"].view(np.uint8)).to(dev, non_blocking=True)
+        arrs = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev, non_blocking=True)
+                for k in ("tile_item", "tile_start", "tile_count", "tile_row", "blk_item", "blk_role")}
+        lib = nat.load()
+        s = nat.stream_handle()
+        max_dim = int(max(r.n_dim for r in act))
+        nat.check(lib.vf_batch_sample(nat.ptr(items), nat.ptr(arrs["tile_item"]), nat.ptr(arrs["tile_start"]),
+                                      nat.ptr(arrs["tile_count"]), nat.ptr(arrs["tile_row"]), t["n_tiles"],
+                                      max_dim, nat.ptr(self._queue), nat.ptr(self.calls), nat.ptr(self.grids),
+                                      nat.ptr(self.params), nat.ptr(self.partials), self.seed,
+                                      nat.ptr(self._flags), self.blocks, s))
+        nat.check(lib.vf_batch_iteration_end(nat.ptr(items), nat.ptr(arrs["blk_item"]), nat.ptr(arrs["blk_role"]),
+                                             int(t["blk_item"].size), nat.ptr(arrs["tile_row"]),
+                                             nat.ptr(self.partials), nat.ptr(self.grids), nat.ptr(self.history),
+                                             nat.ptr(self.avg), self.hist_cap, nat.ptr(self.iters),
+                                             nat.ptr(self.calls), nat.ptr(self._queue), nat.ptr(self._flags), s))
+        slots = torch.as_tensor([r.slot for r in act], dtype=torch.int64, device=dev)
+        state = torch.cat([self.avg[slots][:, 2:4].reshape(-1),
+                           self.iters[slots].to(torch.float64)]).cpu().numpy()
+        now = now_fn()
+        n = len(act)
+        means = state[: 2 * n: 2]
+        sigmas = state[1: 2 * n: 2]
+        its = state[2 * n:].astype(np.int64)
+        self.events_done += int(sum(r.n_events for r in act))
+        self.steps += 1
+        still = []
+        for r, m, sg, it in zip(act, means, sigmas, its):
+            r.iterations = int(it)
+            r.result, r.sigma = float(m), float(sg)
+            conv = math.isfinite(m) and math.isfinite(sg) and m != 0.0 and sg / abs(m) <= r.target_rel_sigma
+            if conv or it >= r.max_iterations:
+                r.converged = bool(conv)
+                r.finished = now
+                self.free_slots.append(r.slot)
+                self.bytes_in_use -= r._footprint
+                self.done.append(r)
+            else:
+                still.append(r)
+        self.active = still
+
+    # ---------------------------------------------------------------- the loop
+    def run(self, requests, realtime=True, time_limit=None):
+        """Serve ``requests`` (sorted by arrival).  With ``realtime`` the arrival
+        times are wall-clock offsets from the start; requests are admitted when
+        they have arrived.  Returns the metrics dict."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        for i, r in enumerate(pending):
+            if r.rid < 0:
+                r.rid = i
+        t0 = time.perf_counter()
+        now_fn = (lambda: time.perf_counter() - t0) if realtime else (lambda: float("inf"))
+        pi = 0
+        busy = 0.0
+        while pi < len(pending) or self.waiting or self.active:
+            now = now_fn()
+            while pi < len(pending) and pending[pi].arrival <= now:
+                self.submit(pending[pi])
+                pi += 1
+            if self.waiting:
+                self._admit(now)
+            if not self.active:
+                if pi < len(pending):
+                    wait = pending[pi].arrival - now_fn()
+                    if wait > 0:
+                        time.sleep(min(wait, 0.01))
+                    continue
+                if self.waiting:
+                    raise RuntimeError("a waiting request does not fit the HBM budget or the slot pool")
+                break
+            ts = time.perf_counter()
+            self.step(now_fn)
+            busy += time.perf_counter() - ts
+            if time_limit is not None and now_fn() > time_limit:
+                break
+        wall = time.perf_counter() - t0
+        if not realtime:
+            for r in self.done:
+                r.finished = r.arrival  # no clock: latencies are not measured
+        lat = [r.latency for r in self.done]
+        flags = int(self._flags.item())
+        return {"requests": len(self.done), "converged": int(sum(r.converged for r in self.done)),
+                "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99),
+                "mean_latency_s": float(np.mean(lat)) if lat else float("nan"),
+                "events": self.events_done, "wall_s": wall, "busy_s": busy,
+                "events_per_s": self.events_done / wall if wall > 0 else float("nan"),
+                "steps": self.steps, "flags": flags}
+
+
+def poisson_workload(rate=200.0, duration=60.0, seed=9, bw_fraction=0.2, target_rel_sigma=1e-3,
+                     max_iterations=20):
+    """Synthetic request stream: Poisson arrivals at ``rate``/s over ``duration``
+    seconds; each request a per-dimension Gaussian (n_dim ~ U{2..16}, events ~
+    10^U[4,7], mu ~ U[0.3,0.7], a ~ U[0.05,0.2]), a fraction replaced by the 6-D
+    Breit-Wigner x linear integrand (c_d from seed 3, 2e6 events)."""
+    from .integrands import breit_wigner, gauss
+
+    rng = np.random.default_rng(seed)
+    c = np.random.default_rng(3).random(5)
+    t = 0.0
+    reqs = []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        if rng.random() < bw_fraction:
+            reqs.append(Request(6, 2_000_000, breit_wigner(c), target_rel_sigma, max_iterations, t))
+        else:
+            d = int(rng.integers(2, 17))
+            n = int(10 ** rng.uniform(4, 7))
+            reqs.append(Request(d, n, gauss(rng.uniform(0.3, 0.7, d), rng.uniform(0.05, 0.2, d)),
+                                target_rel_sigma, max_iterations, t))
+    for i, r in enumerate(reqs):
+        r.rid = i
+    return reqs
