@@ -260,6 +260,8 @@ struct BatchEndArgs {
 
 __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a) {
   const int t = threadIdx.x;
+  // re-arm the sampler's work queue (the sampler launch has completed: stream order)
+  if (blockIdx.x == 0 && t == 0) *a.queue = 0;
   const int item = a.blk_item[blockIdx.x];
   const int role = a.blk_role[blockIdx.x];
   const BatchItem it = a.items[item];
@@ -322,7 +324,6 @@ __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a)
     if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
     a.iters[slot] = iter + 1;
     a.calls[slot] += 1u;
-    if (blockIdx.x == 0) *a.queue = 0;  // the sampler has finished (stream order)
   }
 }
 
