@@ -69,6 +69,9 @@ def _parse():
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--events", type=int, default=EVENTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serving-seconds", type=float, default=10.0,
+                    help="arrival window of the served Poisson stream (0 = skip; the full run is 60)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 1,024-integral batched run")
     return ap.parse_args()
 
 
@@ -343,6 +346,10 @@ def main():
         "gpu_launches": 2 * K,
         "clocks": clk,
     }
+    if not args.no_batched:
+        line["batched"] = batched_run(dev)
+    if args.serving_seconds > 0:
+        line["serving"] = serving_run(args.serving_seconds)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = host_threads()
         cpu_oracle_rate(500_000, threads)
@@ -357,6 +364,60 @@ def main():
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def batched_run(dev, n_iter=5):
+    """C4: 1,024 Gaussians (dims 2-16, 1e4-1e7 events) with their own grids, 5
+    iterations as CUDA-graph replays of the batched fp32 engine, against the
+    float64 single-integral path run one integral after another on a sample."""
+    import numpy as np
+    import torch
+
+    from vegasflow_gb300 import VegasFlow
+    from vegasflow_gb300.batch import VegasBatch, c4_specs
+
+    specs = c4_specs()
+    b = VegasBatch(specs, seed=11)
+    b.run(1, graph=True)
+    b.reset_average()
+    torch.cuda.synchronize()
+    a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    b.run(n_iter, graph=True)
+    c.record()
+    torch.cuda.synchronize()
+    t = a.elapsed_time(c) / 1e3
+    ev = b.total_events() * n_iter
+    # float64 one by one, on every 16th integral (64 of them)
+    sample = specs[::16]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for d, n, f in sample:
+        inst = VegasFlow(d, n, verbose=False, precision="fp64", seed=11, device=dev)
+        inst.compile(f)
+        inst.run_integration(n_iter)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    ev64 = sum(n for _, n, _ in sample) * n_iter
+    return {"workload": "1,024 Gaussians, dims 2-16, 1e4-1e7 events/iteration, own grids, 5 iterations",
+            "integrals": len(specs), "events_per_iteration": b.total_events(),
+            "fp32_batched_events_per_s": ev / t, "ms_per_iteration": 1e3 * t / n_iter,
+            "graph": True, "launches_per_iteration": 2,
+            "fp64_one_by_one_events_per_s": ev64 / t64,
+            "fp64_sample": f"{len(sample)} of the 1,024 integrals, run_integration({n_iter}) each"}
+
+
+def serving_run(seconds):
+    """C5: Poisson arrivals at 200/s (seed 9), 20% Breit-Wigner, target relative
+    sigma 1e-3, at most 20 iterations, 150 GB admission budget, real time."""
+    from vegasflow_gb300.serving import VegasServer, poisson_workload
+
+    reqs = poisson_workload(rate=200.0, duration=seconds, seed=9)
+    server = VegasServer(max_slots=4096, hbm_budget=150e9, seed=9)
+    m = server.run(reqs, realtime=True)
+    m["arrival_window_s"] = seconds
+    m["rate_per_s"] = 200.0
+    return m
 
 
 def e2e_run(inst, K, dev):
