@@ -241,6 +241,25 @@ int vf_vegas_iteration_static(int precision, double* grid, int n_dim, long long 
                               const double* params, int train, double* res_sigma, void* stream);
 
 /*
+ * User integrands as CUDA device functions (replaces the TF custom-op route of
+ * examples/cuda/integrand.cpp:41-89 and the cffi route of
+ * examples/simgauss_cffi.py:25-61).  `source` defines
+ *     __device__ vf_real NAME(const vf_real* x, int n_dim, vf_real weight, const double* params)
+ * where vf_real is double (VF_PREC_F64) or float (VF_PREC_F32), x the event's
+ * point (integration limits applied), weight its full weight, params the
+ * vf_sample `params` pointer.  NVRTC compiles it with the sampler into a kernel
+ * for (alg, precision, n_dim) -- the fp32 VEGAS kernel specialised on n_dim, or
+ * the generic sampler -- built for sm_103a and loaded into the current context;
+ * *integrand_id (>= VF_INT_JIT_BASE) then selects it in vf_sample.  This call
+ * compiles on the host and loads a module: it is not for hot paths.
+ */
+int vf_jit_integrand(const char* source, const char* func_name, int alg, int precision, int n_dim,
+                     int* integrand_id);
+/* Compile only (no GPU needed): VF_OK, or VF_ERR_JIT with the NVRTC log in `log`. */
+int vf_jit_check(const char* source, const char* func_name, int alg, int precision, int n_dim, char* log,
+                 int log_size);
+
+/*
  * Process-wide tunables picked by the autotuner (no counterpart in the
  * reference, whose kernels are TensorFlow's).  Values apply to later launches.
  */

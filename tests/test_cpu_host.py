@@ -154,3 +154,28 @@ def test_plus_host_state():
     assert inst._events_limit == 2_000_000
     inst2 = VegasFlowPlus(14, 100_000, adaptive=True, device="cpu")
     assert inst2._adaptive is False and inst2.n_hypercubes == 1
+
+
+CAMEL_SRC = """
+__device__ vf_real camel(const vf_real* x, int n_dim, vf_real weight, const double* params) {
+  vf_real s1 = 0, s2 = 0;
+  for (int d = 0; d < n_dim; ++d) {
+    const vf_real t1 = (x[d] - (vf_real)params[0]) / (vf_real)params[2];
+    const vf_real t2 = (x[d] - (vf_real)params[1]) / (vf_real)params[2];
+    s1 += t1 * t1;
+    s2 += t2 * t2;
+  }
+  return exp(-s1) + exp(-s2);
+}
+"""
+
+
+def test_cuda_integrand_compiles_without_gpu():
+    """NVRTC compiles the user source with the sampler on the host."""
+    f = integrands.cuda_integrand(CAMEL_SRC, "camel", params=[0.3, 0.7, 0.1])
+    for alg, prec in ((0, 1), (0, 0), (1, 1), (1, 0)):
+        ok, log = f.check(alg, prec, 5)
+        assert ok, log
+    bad = integrands.cuda_integrand("__device__ vf_real bad(const vf_real* x) { return y; }", "bad")
+    ok, log = bad.check()
+    assert not ok and "undefined" in log

@@ -26,7 +26,7 @@ LIB = os.path.join(BUILD, "libvegasgb.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              f"-I{INCLUDE}", f"-I{CSRC}"]
+              f"-I{INCLUDE}", f"-I{CSRC}", f"-I{BUILD}"]
 
 
 def nvcc_path():
@@ -67,9 +67,32 @@ def _compile(src, obj, verbose, extra):
     return obj
 
 
+JIT_HEADERS = ("vf_device.cuh", "vf_sample.cuh", "vf_vegas_f32.cuh")
+
+
+def write_jit_sources():
+    """Embed the sampler headers as strings for NVRTC (``_build/vf_jit_sources.h``)."""
+    out = os.path.join(BUILD, "vf_jit_sources.h")
+    parts = ["// Generated by vegasflow_gb300/build.py: the sampler headers for NVRTC.", "#pragma once",
+             f"static const int kJitHeaderCount = {len(JIT_HEADERS)};",
+             "static const char* kJitHeaderNames[] = {" + ", ".join(f'"{h}"' for h in JIT_HEADERS) + "};",
+             "static const char* kJitHeaderSources[] = {"]
+    for h in JIT_HEADERS:
+        text = open(os.path.join(CSRC, h)).read()
+        assert ")VFJIT\"" not in text
+        parts.append('R"VFJIT(' + text + ')VFJIT",')
+    parts.append("};")
+    new = "\n".join(parts) + "\n"
+    if not os.path.exists(out) or open(out).read() != new:
+        with open(out, "w") as f:
+            f.write(new)
+    return out
+
+
 def build(force=False, verbose=False, jobs=None, extra_flags=()):
     """Compile and link libvegasgb.so; returns its path."""
     os.makedirs(BUILD, exist_ok=True)
+    write_jit_sources()
     srcs = _sources()
     hdr_time = _newest(_headers())
     todo = []
@@ -86,8 +109,7 @@ def build(force=False, verbose=False, jobs=None, extra_flags=()):
         home = cuda_home()
         lib64 = os.path.join(home, "lib64")
         cmd = [nvcc_path(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs,
-               f"-L{lib64}", "-lcudart", "-lnvrtc", "-lcuda", f"-L{os.path.join(lib64, 'stubs')}",
-               "-Xlinker", f"-rpath={lib64}"]
+               f"-L{lib64}", "-lcudart", "-lnvrtc", "-Xlinker", f"-rpath={lib64}"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

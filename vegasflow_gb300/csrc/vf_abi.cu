@@ -168,7 +168,8 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   if (alg == VF_ALG_VEGAS && !grid) return fail(VF_ERR_ARG, "vf_sample: grid is NULL");
   if ((xmin == nullptr) != (xdelta == nullptr))
     return fail(VF_ERR_ARG, "vf_sample: xmin and xdelta must both be given or both NULL");
-  if (!builtin_integrand(integrand)) return fail(VF_ERR_ARG, "vf_sample: unknown integrand %d", integrand);
+  const bool jit = integrand >= VF_INT_JIT_BASE;
+  if (!builtin_integrand(integrand) && !jit) return fail(VF_ERR_ARG, "vf_sample: unknown integrand %d", integrand);
   if ((integrand == VF_INT_SYMGAUSS || integrand == VF_INT_GAUSS || integrand == VF_INT_BREIT_WIGNER) &&
       !params)
     return fail(VF_ERR_ARG, "vf_sample: integrand %d needs params", integrand);
@@ -176,9 +177,10 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
     return fail(VF_ERR_ARG, "vf_sample: partials/rows required when evaluating");
   if (rows < 1) rows = 1;
   const bool taps = ind_out || x_out || w_out || f_out;
-  const bool fast = use_vegas_f32(alg, precision, integrand, taps);
-  const void* k = fast ? vf::vegas_f32_kernel(n_dim, integrand) : sample_kernel(precision, n_dim, integrand);
-  if (!k) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no kernel for this configuration");
+  const bool fast = !jit && use_vegas_f32(alg, precision, integrand, taps);
+  const void* k = jit ? nullptr
+                      : (fast ? vf::vegas_f32_kernel(n_dim, integrand) : sample_kernel(precision, n_dim, integrand));
+  if (!k && !jit) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no kernel for this configuration");
 
   vf::SampleArgs a;
   a.grid = grid;
@@ -203,6 +205,16 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   a.train = train ? 1 : 0;
   a.accumulate = accumulate ? 1 : 0;
   fill_philox(a, seed, call_ctr);
+  if (jit) {
+    if (taps && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS)
+      return fail(VF_ERR_UNSUPPORTED, "vf_sample: a JIT fp32 VEGAS integrand has no per-event taps");
+    int fast_jit = 0;
+    a.hist_copies = g_f32_hist_copies.load();
+    const int rc = vf::jit_launch(integrand, alg, precision, n_dim, &a, rows, a.train, stream, &fast_jit,
+                                  &a.hist_copies);
+    (void)fast_jit;
+    return rc ? rc : check_launch("vf_sample (JIT)");
+  }
   int smem;
   if (fast) {
     a.hist_copies = g_f32_hist_copies.load();

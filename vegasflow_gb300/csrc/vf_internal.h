@@ -20,6 +20,12 @@ inline const void* vegas_f32_kernel(int n_dim, int integrand) {
   return n_dim <= 8 ? vegas_f32_kernel_a(n_dim, integrand) : vegas_f32_kernel_b(n_dim, integrand);
 }
 
+// Launches the NVRTC-compiled sampler of a JIT integrand with `args` (a
+// SampleArgs); reports whether it is the fp32 VEGAS kernel and settles the
+// histogram layout it uses.
+int jit_launch(int integrand_id, int alg, int precision, int n_dim, void* args, int rows, int train,
+               void* stream, int* fast_out, int* hist_copies_inout);
+
 // Records an error message for vf_last_error_string(); returns `code`.
 int set_error(int code, const char* message);
 

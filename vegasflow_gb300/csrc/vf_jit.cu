@@ -1,0 +1,206 @@
+// NVRTC-compiled user integrands.
+//
+// A user integrand is CUDA source defining a device function
+//     vf_real f(const vf_real* x, int n_dim, vf_real weight, const double* params)
+// (vf_real = the sampler's precision, typedef'd before the source).  It is
+// compiled together with the sampler headers (embedded in the library) into a
+// sampler kernel specialised for the integrand: the fp32 VEGAS kernel on the
+// exact dimension count, or the generic sampler for float64 and plain MC.
+// The CUBIN is built for sm_103a and loaded with the driver API; launches go
+// through vf_sample with the returned integrand id.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vegasflow_gb300.h"
+#include "vf_internal.h"
+#include "vf_jit_sources.h"
+#include "vf_vegas_f32.cuh"
+
+namespace {
+
+// Driver entry points, resolved through the runtime (no link-time dependency on
+// the driver library, so the library loads on machines without a GPU driver).
+typedef CUresult (*PfnModuleLoadData)(CUmodule*, const void*);
+typedef CUresult (*PfnModuleGetFunction)(CUfunction*, CUmodule, const char*);
+typedef CUresult (*PfnLaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                                    unsigned, CUstream, void**, void**);
+typedef CUresult (*PfnFuncSetAttribute)(CUfunction, CUfunction_attribute, int);
+
+struct Driver {
+  PfnModuleLoadData module_load_data = nullptr;
+  PfnModuleGetFunction module_get_function = nullptr;
+  PfnLaunchKernel launch_kernel = nullptr;
+  PfnFuncSetAttribute func_set_attribute = nullptr;
+  bool ok = false;
+};
+
+const Driver& driver() {
+  static Driver d;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    auto get = [](const char* name, void** fn) {
+      cudaDriverEntryPointQueryResult q;
+      return cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+             q == cudaDriverEntryPointSuccess && *fn != nullptr;
+    };
+    d.ok = get("cuModuleLoadData", reinterpret_cast<void**>(&d.module_load_data)) &&
+           get("cuModuleGetFunction", reinterpret_cast<void**>(&d.module_get_function)) &&
+           get("cuLaunchKernel", reinterpret_cast<void**>(&d.launch_kernel)) &&
+           get("cuFuncSetAttribute", reinterpret_cast<void**>(&d.func_set_attribute));
+  });
+  return d;
+}
+
+struct JitKernel {
+  CUmodule module = nullptr;
+  CUfunction fn = nullptr;
+  int alg = 0, precision = 0, n_dim = 0, fast = 0, smem_set = 0;
+};
+
+std::mutex g_mu;
+std::vector<JitKernel> g_kernels;
+
+std::string program_text(const char* source, const char* func_name, int alg, int precision, int n_dim,
+                         std::string* expr) {
+  const bool fast = precision == VF_PREC_F32 && alg == VF_ALG_VEGAS;
+  std::string src = "#define VF_JIT_USER 1\n";
+  src += std::string("typedef ") + (precision == VF_PREC_F64 ? "double" : "float") + " vf_real;\n";
+  src += source;
+  src += "\n#define VF_USER_FN " + std::string(func_name) + "\n";
+  src += fast ? "#include \"vf_vegas_f32.cuh\"\n" : "#include \"vf_sample.cuh\"\n";
+  if (fast) {
+    *expr = "vf::vf_vegas_f32_kernel<" + std::to_string(n_dim) + ", 99>";
+  } else {
+    *expr = std::string("vf::vf_sample_kernel<") + (precision == VF_PREC_F64 ? "double" : "float") + ", " +
+            std::to_string(vf::dim_bucket(n_dim)) + ", 99>";
+  }
+  return src;
+}
+
+// Compile; on success returns the CUBIN and the lowered kernel name.
+int compile(const char* source, const char* func_name, int alg, int precision, int n_dim, std::vector<char>* cubin,
+            std::string* lowered, std::string* log) {
+  if (!source || !func_name || !*func_name) return VF_ERR_ARG;
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return VF_ERR_UNSUPPORTED;
+  if ((alg != VF_ALG_VEGAS && alg != VF_ALG_PLAIN) || (precision != VF_PREC_F64 && precision != VF_PREC_F32))
+    return VF_ERR_ARG;
+  std::string expr;
+  const std::string src = program_text(source, func_name, alg, precision, n_dim, &expr);
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "vf_user_integrand.cu", kJitHeaderCount, kJitHeaderSources,
+                         kJitHeaderNames) != NVRTC_SUCCESS)
+    return VF_ERR_JIT;
+  nvrtcAddNameExpression(prog, expr.c_str());
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
+  const nvrtcResult rc = nvrtcCompileProgram(prog, 3, opts);
+  size_t log_size = 0;
+  nvrtcGetProgramLogSize(prog, &log_size);
+  if (log && log_size > 1) {
+    log->resize(log_size);
+    nvrtcGetProgramLog(prog, &(*log)[0]);
+  }
+  if (rc != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    return VF_ERR_JIT;
+  }
+  const char* name = nullptr;
+  nvrtcGetLoweredName(prog, expr.c_str(), &name);
+  if (lowered && name) *lowered = name;
+  if (cubin) {
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    cubin->resize(n);
+    nvrtcGetCUBIN(prog, cubin->data());
+  }
+  nvrtcDestroyProgram(&prog);
+  return VF_OK;
+}
+
+}  // namespace
+
+namespace vf {
+
+// Launch a JIT kernel for vf_sample (declared in vf_internal.h).
+int jit_launch(int integrand_id, int alg, int precision, int n_dim, void* args, int rows, int train, void* stream,
+               int* fast_out, int* hist_copies_inout) {
+  JitKernel k;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    const int idx = integrand_id - VF_INT_JIT_BASE;
+    if (idx < 0 || idx >= (int)g_kernels.size()) return set_error(VF_ERR_ARG, "unknown JIT integrand id");
+    k = g_kernels[idx];
+  }
+  if (k.alg != alg || k.precision != precision || k.n_dim != n_dim)
+    return set_error(VF_ERR_ARG, "JIT integrand was compiled for another algorithm, precision or n_dim");
+  *fast_out = k.fast;
+  int smem;
+  if (k.fast) {
+    smem = vegas_f32_smem_bytes(n_dim, *hist_copies_inout, train);
+  } else {
+    *hist_copies_inout = precision == VF_PREC_F32 ? 8 : 1;
+    smem = sample_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, *hist_copies_inout,
+                             train && alg == VF_ALG_VEGAS);
+  }
+  const Driver& drv = driver();
+  if (!drv.ok) return set_error(VF_ERR_CUDA, "CUDA driver entry points unavailable");
+  if (smem > 48 * 1024 &&
+      drv.func_set_attribute(k.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS)
+    return set_error(VF_ERR_CUDA, "cuFuncSetAttribute for a JIT kernel failed");
+  void* params[] = {args};
+  const CUresult r =
+      drv.launch_kernel(k.fn, rows, 1, 1, VF_THREADS, 1, 1, smem, (CUstream)stream, params, nullptr);
+  if (r != CUDA_SUCCESS) return set_error(VF_ERR_LAUNCH, "cuLaunchKernel failed for a JIT kernel");
+  return VF_OK;
+}
+
+}  // namespace vf
+
+extern "C" {
+
+int vf_jit_check(const char* source, const char* func_name, int alg, int precision, int n_dim, char* log,
+                 int log_size) {
+  std::string lg;
+  const int rc = compile(source, func_name, alg, precision, n_dim, nullptr, nullptr, &lg);
+  if (log && log_size > 0) {
+    const size_t n = lg.size() < (size_t)log_size - 1 ? lg.size() : (size_t)log_size - 1;
+    lg.copy(log, n);
+    log[n] = 0;
+  }
+  if (rc == VF_ERR_JIT) return vf::set_error(rc, ("NVRTC: " + lg).c_str());
+  if (rc) return vf::set_error(rc, "vf_jit_check: bad arguments");
+  return VF_OK;
+}
+
+int vf_jit_integrand(const char* source, const char* func_name, int alg, int precision, int n_dim,
+                     int* integrand_id) {
+  if (!integrand_id) return vf::set_error(VF_ERR_ARG, "vf_jit_integrand: integrand_id is NULL");
+  std::vector<char> cubin;
+  std::string lowered, lg;
+  int rc = compile(source, func_name, alg, precision, n_dim, &cubin, &lowered, &lg);
+  if (rc == VF_ERR_JIT) return vf::set_error(rc, ("NVRTC: " + lg).c_str());
+  if (rc) return vf::set_error(rc, "vf_jit_integrand: bad arguments");
+  if (cudaFree(nullptr) != cudaSuccess)  // make the device's primary context current
+    return vf::set_error(VF_ERR_CUDA, "vf_jit_integrand: no CUDA context");
+  const Driver& drv = driver();
+  if (!drv.ok) return vf::set_error(VF_ERR_CUDA, "vf_jit_integrand: CUDA driver entry points unavailable");
+  JitKernel k;
+  if (drv.module_load_data(&k.module, cubin.data()) != CUDA_SUCCESS)
+    return vf::set_error(VF_ERR_JIT, "vf_jit_integrand: cuModuleLoadData failed");
+  if (drv.module_get_function(&k.fn, k.module, lowered.c_str()) != CUDA_SUCCESS)
+    return vf::set_error(VF_ERR_JIT, "vf_jit_integrand: kernel not found in the module");
+  k.alg = alg;
+  k.precision = precision;
+  k.n_dim = n_dim;
+  k.fast = precision == VF_PREC_F32 && alg == VF_ALG_VEGAS;
+  std::lock_guard<std::mutex> lock(g_mu);
+  g_kernels.push_back(k);
+  *integrand_id = VF_INT_JIT_BASE + (int)g_kernels.size() - 1;
+  return VF_OK;
+}
+
+}  // extern "C"

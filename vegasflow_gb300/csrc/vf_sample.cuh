@@ -81,18 +81,16 @@ __host__ __device__ inline int sample_smem_bytes(int real_size, int D, int hist_
 }
 
 // ----- the integrand call ----------------------------------------------------
-#ifdef VF_JIT_USER
-// Supplied by the user's source, compiled together with this header by NVRTC.
-__device__ Real_user vf_user_integrand(const Real_user* x, int n_dim, Real_user weight,
-                                       const double* params);
-#endif
-
+// VF_USER_FN names the user's device function when NVRTC compiles this header
+// together with the user's source (VF_JIT_USER defined): it is declared before
+// this header as  vf_real f(const vf_real* x, int n_dim, vf_real weight,
+// const double* params)  with vf_real the sampler's precision.
 template <typename Real, int DMAX, int INTEG>
 __device__ __forceinline__ Real call_integrand(const Real* x, int D, Real w,
                                                const IntegrandConsts<Real, DMAX>& k,
                                                const double* __restrict__ params) {
 #ifdef VF_JIT_USER
-  if constexpr (INTEG == VF_INT_USER) return vf_user_integrand(x, D, w, params);
+  if constexpr (INTEG == VF_INT_USER) return (Real)VF_USER_FN(x, D, w, params);
 #endif
   return eval_builtin<DMAX>(INTEG, x, D, k);
 }
@@ -167,6 +165,7 @@ vf_sample_kernel(const SampleArgs a) {
   const double xdeltajac = a.xdeltajac;
   // float64 factor of the fp32 form's weight: 50^D (VEGAS Jacobian constant) * xjac * prod(xdelta)
   const double wscale = (sizeof(Real) == 8) ? 1.0 : (vegas ? pow(50.0, (double)D) : 1.0) * xjac * xdeltajac;
+  const float wscale_f = (float)wscale;
 
   double acc1 = 0.0, acc2 = 0.0;  // fp64 accumulators
   F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};  // fp32 compensated accumulators
@@ -310,7 +309,7 @@ vf_sample_kernel(const SampleArgs a) {
       }
       w = (Real)wf;  // the weight without its constant factor (applied in float64 later)
       if (evaluate) {
-        const float f = (float)call_integrand<Real, DMAX, INTEG>(x, D, w, kc, a.params);
+        const float f = (float)call_integrand<Real, DMAX, INTEG>(x, D, (Real)(wf * wscale_f), kc, a.params);
         const float v = wf * f;
         const float v2 = v * v;
         two_sum_add(s1, v);

@@ -113,8 +113,9 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   // float64 constant of the weight (host-computed): 50^D * xjac, times
   // pref / prod k for the Gaussian family
   const double wscale = g_wscale;
+  const float wscale_f = (float)wscale;  // the full weight handed to a user integrand
   IntegrandConsts<float, D> kc;
-  if (!GAUSS) load_consts<D>(kc, INTEG, a.params, D);
+  if (!GAUSS) load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
 
   float* my_hist = hist + (warp * cpw + ((lane * cpw) >> 5)) * NB;
   F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
@@ -122,10 +123,16 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   // one event from its per-dimension (bin, m) pairs
   auto finish = [&](const int (&bins)[D], float wf, float s, const float (&x)[D]) {
     float f;
-    if (GAUSS)
+    if constexpr (GAUSS) {
       f = ex2_approx_ftz(-s);
-    else
-      f = eval_builtin<D>(INTEG, x, D, kc);
+    } else {
+#ifdef VF_JIT_USER
+      if constexpr (INTEG == VF_INT_USER)
+        f = (float)VF_USER_FN(x, D, wf * wscale_f, a.params);
+      else
+#endif
+        f = eval_builtin<D>(INTEG, x, D, kc);
+    }
     const float v = wf * f;
     const float v2 = v * v;
     two_sum_add(s1, v);

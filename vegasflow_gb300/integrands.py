@@ -8,9 +8,9 @@ per-dimension Gaussian, Breit-Wigner times linear factors) and two simple
 test integrands; ``cuda_integrand`` JIT-compiles a user's CUDA device function
 into the same sampler.
 
-Each object is also callable on torch tensors with the reference's integrand
-signature ``f(xarr, weight=None, n_dim=None)`` (same formula, evaluated by
-torch), which the tests use as the plain float64 comparison.
+Each built-in object is also callable on torch tensors with the reference's
+integrand signature ``f(xarr, weight=None, n_dim=None)`` (same formula,
+evaluated by torch), which the tests use as the plain float64 comparison.
 """
 
 from __future__ import annotations
@@ -133,3 +133,50 @@ def prod():
 def sum_():
     """sum_d x_d (the examples/cuda custom-op integrand)."""
     return DeviceIntegrand(nat.VF_INT_SUM, "sum", None, lambda x: torch.sum(x, dim=1))
+
+
+class CudaIntegrand(DeviceIntegrand):
+    """A user integrand written as a CUDA device function, compiled by NVRTC into
+    the sampler (one specialised kernel per algorithm, precision and dimension
+    count, compiled on first use and cached).
+
+    ``source`` defines ``__device__ vf_real NAME(const vf_real* x, int n_dim,
+    vf_real weight, const double* params)`` where ``vf_real`` is ``double`` or
+    ``float`` following the integrator's precision; ``params`` (optional floats)
+    reach the function as a device array.  ``torch_fn`` optionally gives the same
+    integrand on torch tensors (for checks)."""
+
+    def __init__(self, source, name, params=None, torch_fn=None, n_dim=None):
+        super().__init__(-1, name, None, torch_fn, n_dim)
+        self.source = source
+        self._user_params = None if params is None else np.asarray(params, dtype=np.float64)
+        self._ids = {}
+
+    def params(self, n_dim):
+        return self._user_params if self._user_params is not None else np.zeros(1)
+
+    def compile_for(self, alg, precision, n_dim):
+        """The integrand id of the kernel for (alg, precision, n_dim), compiling it if needed."""
+        import ctypes
+
+        key = (alg, precision, n_dim)
+        if key not in self._ids:
+            out = ctypes.c_int(0)
+            nat.check(nat.load().vf_jit_integrand(self.source.encode(), self.__name__.encode(), alg, precision,
+                                                  n_dim, ctypes.byref(out)))
+            self._ids[key] = out.value
+        return self._ids[key]
+
+    def check(self, alg=0, precision=1, n_dim=4):
+        """Compile without a GPU; returns (ok, NVRTC log)."""
+        import ctypes
+
+        buf = ctypes.create_string_buffer(1 << 16)
+        rc = nat.load().vf_jit_check(self.source.encode(), self.__name__.encode(), alg, precision, n_dim, buf,
+                                     len(buf))
+        return rc == nat.VF_OK, buf.value.decode(errors="replace")
+
+
+def cuda_integrand(source, name, params=None, torch_fn=None, n_dim=None):
+    """Build a ``CudaIntegrand`` (see its docstring)."""
+    return CudaIntegrand(source, name, params, torch_fn, n_dim)

@@ -405,6 +405,9 @@ class MonteCarloFlow(ABC):
             integrand.check_dims(self.n_dim)
             self._kind = "device"
             self._int_id = integrand.integrand_id
+            if getattr(integrand, "source", None) is not None:  # CUDA source: NVRTC on first use
+                if self.device.type == "cuda":
+                    self._int_id = self._compile_cuda_integrand(integrand)
             self._params_host = integrand.params(self.n_dim)
             self._params_dev = torch.as_tensor(self._params_host, dtype=torch.float64,
                                                device=self.device) if self.device.type == "cuda" else None
@@ -458,6 +461,9 @@ class MonteCarloFlow(ABC):
             self._ws.clear()
         if trace:
             self.trace(n_events=23)
+
+    def _compile_cuda_integrand(self, integrand):
+        return integrand.compile_for(self._ALG, self._prec, self.n_dim)
 
     def _choose_rows(self):
         lib = nat.load()

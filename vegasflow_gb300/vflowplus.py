@@ -112,6 +112,10 @@ class VegasFlowPlus(VegasFlow):
         self._ev_start[0] = 0
         self._n_ev_stale = True
 
+    def _compile_cuda_integrand(self, integrand):
+        raise NotImplementedError("VegasFlowPlus evaluates built-in device integrands and torch callables; "
+                                  "CUDA-source integrands run with VegasFlow and PlainFlow")
+
     def _plus_rows(self):
         import ctypes
         rows = ctypes.c_int(0)
