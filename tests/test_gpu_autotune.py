@@ -1,0 +1,83 @@
+"""Launch-shape autotuner on the GPU: every launch shape gives the same
+integral (the Philox stream is per event, so only summation order and the
+histogram's float atomics differ), and ``autotune=True`` picks one, caches it
+and integrates correctly with it."""
+
+import numpy as np
+import pytest
+
+from vegasflow_gb300 import VegasFlow, autotune, integrands
+
+pytestmark = pytest.mark.gpu
+
+N_DIM = 6
+N_EVENTS = 2_000_000
+
+
+def _run(shape, n_iter=3, train=True, seed=123):
+    inst = VegasFlow(N_DIM, N_EVENTS, precision="fp32", seed=seed, verbose=False, train=train)
+    inst.compile(integrands.symgauss())
+    inst.set_launch_shape(shape)
+    first = inst.run_integration(1)
+    res, sig = inst.run_integration(n_iter)
+    return first, res, sig, inst
+
+
+@pytest.mark.parametrize("shape", [autotune.LaunchShape(128, 0, 0), autotune.LaunchShape(256, 1, 4),
+                                   autotune.LaunchShape(128, 2, 2), autotune.LaunchShape(256, 2, 1)])
+def test_shapes_agree(shape):
+    (r0, s0), res0, sig0, _ = _run(None)
+    (r1, s1), res1, sig1, inst = _run(shape)
+    assert inst.launch_shape == shape
+    # first iteration: identical events on the initial grid, different summation order
+    assert abs(r1 - r0) <= 1e-6 * abs(r0)
+    assert abs(s1 - s0) <= 1e-4 * s0
+    # later iterations: the grid refines from histograms that differ by float rounding
+    assert abs(res1 - res0) < 0.5 * sig0
+    assert abs(res1 - 1.0) < 5 * sig1
+
+
+def test_frozen_grid_shapes_agree():
+    (r0, _), res0, _, _ = _run(None, train=False)
+    (r1, _), res1, _, _ = _run(autotune.LaunchShape(128, 1, 0), train=False)
+    assert abs(r1 - r0) <= 1e-6 * abs(r0)
+    assert abs(res1 - res0) <= 1e-6 * abs(res0)
+
+
+def test_autotune_picks_and_caches(tmp_path, monkeypatch):
+    path = tmp_path / "shapes.json"
+    monkeypatch.setenv("VEGASFLOW_GB300_TUNE_CACHE", str(path))
+    saved = autotune.current()
+    inst = VegasFlow(N_DIM, N_EVENTS, precision="fp32", seed=5, verbose=False, autotune=True)
+    inst.compile(integrands.symgauss())
+    shape = inst.launch_shape
+    assert shape in autotune.candidates(train=True)
+    assert autotune.current() == shape  # applied for this integrator's launches
+    cache = autotune.TuneCache(str(path))
+    assert len(cache.entries) == 1
+    entry = next(iter(cache.entries.values()))
+    assert entry["ms"] <= entry["default_ms"] * 1.0001
+    res, sig = inst.run_integration(4)
+    assert abs(res - 1.0) < 5 * sig
+    # a second integrator of the same workload reads the cache (no re-timing)
+    cache_mtime = path.stat().st_mtime_ns
+    again = VegasFlow(N_DIM, N_EVENTS, precision="fp32", seed=6, verbose=False, autotune=True)
+    again.compile(integrands.symgauss())
+    assert again.launch_shape == shape
+    assert path.stat().st_mtime_ns == cache_mtime
+    # an untuned integrator interleaved with it runs on the default shape
+    plain = VegasFlow(N_DIM, N_EVENTS, precision="fp32", seed=7, verbose=False)
+    plain.compile(integrands.symgauss())
+    plain.run_integration(1)
+    assert autotune.current() == autotune.DEFAULT_SHAPE
+    again.run_integration(1)
+    assert autotune.current() == shape
+    autotune.apply(saved)
+
+
+def test_autotune_is_noop_off_the_fused_path(tmp_path, monkeypatch):
+    monkeypatch.setenv("VEGASFLOW_GB300_TUNE_CACHE", str(tmp_path / "s.json"))
+    inst = VegasFlow(2, 10_000, precision="fp64", seed=1, verbose=False, autotune=True)
+    inst.compile(integrands.symgauss())
+    assert inst.launch_shape is None
+    assert not (tmp_path / "s.json").exists()

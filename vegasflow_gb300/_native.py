@@ -41,6 +41,8 @@ VF_INT_SUM = 5
 VF_INT_JIT_BASE = 1000
 
 VF_TUNE_F32_HIST_COPIES = 1
+VF_TUNE_F32_THREADS = 2
+VF_TUNE_F32_BLOCKS_PER_SM = 3
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int

@@ -16,6 +16,11 @@ namespace {
 // Tunables (vf_tune_set): histogram copies per warp of the fp32 VEGAS sampler.
 // 0 = joint pair tables, 1|2|4 = per-dimension tables with that many copies per warp.
 std::atomic<int> g_f32_hist_copies{0};
+// block size of the fp32 VEGAS sampler (128 | 256)
+std::atomic<int> g_f32_threads{256};
+// persistent blocks per SM of the fp32 VEGAS sampler (0 = as many as fit): with
+// the block size it sets the events each thread processes
+std::atomic<int> g_f32_blocks_per_sm{0};
 
 thread_local char g_err[1024] = "";
 
@@ -94,6 +99,16 @@ extern "C" {
 int vf_version(void) { return 1; }
 
 int vf_tune_set(int key, int value) {
+  if (key == VF_TUNE_F32_THREADS) {
+    if (value != 128 && value != 256) return fail(VF_ERR_ARG, "vf_tune_set: threads must be 128 or 256");
+    g_f32_threads.store(value);
+    return VF_OK;
+  }
+  if (key == VF_TUNE_F32_BLOCKS_PER_SM) {
+    if (value < 0 || value > 16) return fail(VF_ERR_ARG, "vf_tune_set: blocks per SM must be 0..16");
+    g_f32_blocks_per_sm.store(value);
+    return VF_OK;
+  }
   if (key == VF_TUNE_F32_HIST_COPIES) {
     if (value != 0 && value != 1 && value != 2 && value != 4)
       return fail(VF_ERR_ARG, "vf_tune_set: histogram layout must be 0 (joint pairs) or 1, 2, 4");
@@ -107,6 +122,14 @@ int vf_tune_get(int key, int* value) {
   if (!value) return fail(VF_ERR_ARG, "vf_tune_get: value is NULL");
   if (key == VF_TUNE_F32_HIST_COPIES) {
     *value = g_f32_hist_copies.load();
+    return VF_OK;
+  }
+  if (key == VF_TUNE_F32_THREADS) {
+    *value = g_f32_threads.load();
+    return VF_OK;
+  }
+  if (key == VF_TUNE_F32_BLOCKS_PER_SM) {
+    *value = g_f32_blocks_per_sm.load();
     return VF_OK;
   }
   return fail(VF_ERR_ARG, "vf_tune_get: unknown key %d", key);
@@ -133,9 +156,12 @@ int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, 
   const int integ = builtin_integrand(integrand) ? integrand : VF_INT_SYMGAUSS;
   const void* k;
   int smem;
-  if (use_vegas_f32(alg, precision, integ, false)) {
-    k = vf::vegas_f32_kernel(n_dim, integ);
-    smem = vf::vegas_f32_smem_bytes(n_dim, g_f32_hist_copies.load(), train);
+  int threads = VF_THREADS;
+  const bool fast = use_vegas_f32(alg, precision, integ, false);
+  if (fast) {
+    threads = g_f32_threads.load();
+    k = vf::vegas_f32_kernel(n_dim, integ, threads);
+    smem = vf::vegas_f32_smem_bytes(n_dim, g_f32_hist_copies.load(), train, threads);
   } else {
     k = sample_kernel(precision, n_dim, integ);
     const int real = precision == VF_PREC_F64 ? 8 : 4;
@@ -145,11 +171,14 @@ int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, 
   int rc = prepare_smem(k, smem);
   if (rc) return rc;
   int per_sm = 0;
-  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, VF_THREADS, smem);
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
   if (e != cudaSuccess) return fail(VF_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
   const int sms = sm_count();
   if (sms <= 0) return fail(VF_ERR_CUDA, "no CUDA device");
-  *rows = (per_sm > 0 ? per_sm : 1) * sms;
+  if (per_sm < 1) per_sm = 1;
+  const int want = fast ? g_f32_blocks_per_sm.load() : 0;
+  if (want > 0 && want < per_sm) per_sm = want;
+  *rows = per_sm * sms;
   return VF_OK;
 }
 
@@ -178,8 +207,10 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   if (rows < 1) rows = 1;
   const bool taps = ind_out || x_out || w_out || f_out;
   const bool fast = !jit && use_vegas_f32(alg, precision, integrand, taps);
+  const int threads = fast ? g_f32_threads.load() : VF_THREADS;
   const void* k = jit ? nullptr
-                      : (fast ? vf::vegas_f32_kernel(n_dim, integrand) : sample_kernel(precision, n_dim, integrand));
+                      : (fast ? vf::vegas_f32_kernel(n_dim, integrand, threads)
+                              : sample_kernel(precision, n_dim, integrand));
   if (!k && !jit) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no kernel for this configuration");
 
   vf::SampleArgs a;
@@ -218,7 +249,7 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   int smem;
   if (fast) {
     a.hist_copies = g_f32_hist_copies.load();
-    smem = vf::vegas_f32_smem_bytes(n_dim, a.hist_copies, a.train);
+    smem = vf::vegas_f32_smem_bytes(n_dim, a.hist_copies, a.train, threads);
   } else {
     a.hist_copies = hist_copies_for(precision);
     const int real = precision == VF_PREC_F64 ? 8 : 4;
@@ -228,7 +259,7 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   if (rc) return rc;
   void* args[] = {&a};
   const cudaError_t e =
-      cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
+      cudaLaunchKernel(k, dim3(rows), dim3(threads), args, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "vf_sample launch: %s", cudaGetErrorString(e));
   return check_launch("vf_sample");
 }

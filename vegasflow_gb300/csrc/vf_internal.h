@@ -13,11 +13,15 @@ const void* plus_kernel_f64(int dmax, int integrand);
 const void* plus_kernel_f32(int dmax, int integrand);
 
 // The fp32 VEGAS sampler specialised on the exact dimension count (1..8 in
-// part a, 9..16 in part b).
-const void* vegas_f32_kernel_a(int n_dim, int integrand);
-const void* vegas_f32_kernel_b(int n_dim, int integrand);
-inline const void* vegas_f32_kernel(int n_dim, int integrand) {
-  return n_dim <= 8 ? vegas_f32_kernel_a(n_dim, integrand) : vegas_f32_kernel_b(n_dim, integrand);
+// part a, 9..16 in part b) and the block size (128 or 256 threads).
+const void* vegas_f32_kernel_a256(int n_dim, int integrand);
+const void* vegas_f32_kernel_b256(int n_dim, int integrand);
+const void* vegas_f32_kernel_a128(int n_dim, int integrand);
+const void* vegas_f32_kernel_b128(int n_dim, int integrand);
+inline const void* vegas_f32_kernel(int n_dim, int integrand, int threads = 256) {
+  if (threads == 128)
+    return n_dim <= 8 ? vegas_f32_kernel_a128(n_dim, integrand) : vegas_f32_kernel_b128(n_dim, integrand);
+  return n_dim <= 8 ? vegas_f32_kernel_a256(n_dim, integrand) : vegas_f32_kernel_b256(n_dim, integrand);
 }
 
 // Launches the NVRTC-compiled sampler of a JIT integrand with `args` (a

@@ -43,15 +43,18 @@ __device__ __forceinline__ float ex2_approx_ftz(float x) {
 
 __host__ __device__ inline int vegas_f32_joint_floats(int D) { return (D / 2) * 2500 + (D & 1) * 50; }
 
-__host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, int train) {
+__host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, int train,
+                                                    int threads = VF_THREADS) {
   const int nb = D * VF_BINS;
   const int hist = copies_per_warp == 0 ? vegas_f32_joint_floats(D) * 4
-                                        : (VF_THREADS / 32) * copies_per_warp * nb * 4;
+                                        : (threads / 32) * copies_per_warp * nb * 4;
   return nb * 8 + (train ? hist : 0);
 }
 
-template <int D, int INTEG>
-__global__ void __launch_bounds__(VF_THREADS, VF_F32_MIN_BLOCKS)
+// THREADS: the block size (an autotuner choice, 128 or 256); the register cap
+// (launch bounds) stays at 64 per thread for both.
+template <int D, int INTEG, int THREADS = VF_THREADS>
+__global__ void __launch_bounds__(THREADS, VF_F32_MIN_BLOCKS * VF_THREADS / THREADS)
 vf_vegas_f32_kernel(const SampleArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NB = D * VF_BINS;
@@ -106,7 +109,7 @@ vf_vegas_f32_kernel(const SampleArgs a) {
     if (cpw == 0)
       for (int k = tid; k < NP * 2500 + (D & 1) * VF_BINS; k += blockDim.x) hist[k] = 0.0f;
     else
-      for (int k = tid; k < (VF_THREADS / 32) * cpw * NB; k += blockDim.x) hist[k] = 0.0f;
+      for (int k = tid; k < (THREADS / 32) * cpw * NB; k += blockDim.x) hist[k] = 0.0f;
   }
   __syncthreads();
 
@@ -218,7 +221,7 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   }
 
   // ---- block partials: TwoSum merges across the warp and the block, float64 row
-  __shared__ double red[2][VF_THREADS / 32];
+  __shared__ double red[2][THREADS / 32];
   s1 = warp_sum(s1);
   s2 = warp_sum(s2);
   if (lane == 0) {
@@ -230,7 +233,7 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   double* row = a.partials + (long long)blockIdx.x * W;
   if (tid == 0) {
     double b1 = 0.0, b2 = 0.0;
-    for (int i = 0; i < VF_THREADS / 32; ++i) {
+    for (int i = 0; i < THREADS / 32; ++i) {
       b1 += red[0][i];
       b2 += red[1][i];
     }
@@ -248,7 +251,7 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   if (train) {
     // marginals / copy sums in fp32 (the tables are fp32), one float64 scaling per bin
     const double s2c = wscale * wscale;
-    const int ncopies = (VF_THREADS / 32) * cpw;
+    const int ncopies = (THREADS / 32) * cpw;
     for (int k = tid; k < NB; k += blockDim.x) {
       float hf = 0.0f;
       if (cpw == 0) {

@@ -36,6 +36,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from . import autotune
 from .configflow import (
     ALPHA,
     BINS_MAX,
@@ -77,10 +78,11 @@ class MonteCarloFlow(ABC):
 
     _CAN_RUN_VECTORIAL = False
     _ALG = nat.VF_ALG_PLAIN
+    _FUSED_F32_SAMPLER = False  # launches the fused fp32 VEGAS sampler (has a launch shape)
 
     def __init__(self, n_dim, n_events, events_limit=MAX_EVENTS_LIMIT,
                  list_devices=DEFAULT_ACTIVE_DEVICES, verbose=True, xmin=None, xmax=None,
-                 precision=None, device=None, seed=None, **kwargs):
+                 precision=None, device=None, seed=None, autotune=False, **kwargs):
         if "simplify_signature" in kwargs:
             logger.warning("simplify_signature is deprecated and will be removed")
         self.n_dim = int(n_dim)
@@ -117,6 +119,8 @@ class MonteCarloFlow(ABC):
         self._rows = 0
         self._ws = {}
         self._it = 0
+        self._autotune = bool(autotune)
+        self._shape = None
 
         if xmin is not None or xmax is not None:  # monte_carlo.py:159-175
             if xmin is None or xmax is None:
@@ -229,16 +233,18 @@ class MonteCarloFlow(ABC):
 
     def _workspace(self):
         ws = self._ws
-        if ws.get("key") != (self._rows, self._width()):
+        if ws.get("key") != self._width():
             ws.clear()
-            ws["key"] = (self._rows, self._width())
-            ws["partials"] = torch.zeros(self._rows * self._width(), dtype=torch.float64,
-                                         device=self.device)
+            ws["key"] = self._width()
             ws["flags"] = torch.zeros(1, dtype=torch.int32, device=self.device)
             ws["history"] = torch.zeros((16, 2 * self._n_out), dtype=torch.float64, device=self.device)
             ws["avg"] = torch.zeros(5 * self._n_out, dtype=torch.float64, device=self.device)
             ws["hist"] = torch.zeros((self.n_dim, BINS_MAX), dtype=torch.float64, device=self.device)
             ws["sums"] = torch.zeros(2 * self._n_out, dtype=torch.float64, device=self.device)
+        if ws.get("rows") != self._rows:  # the launch shape sets the partial-row count
+            ws["rows"] = self._rows
+            ws["partials"] = torch.zeros(self._rows * self._width(), dtype=torch.float64,
+                                         device=self.device)
         return ws
 
     def _history_slot(self):
@@ -282,6 +288,7 @@ class MonteCarloFlow(ABC):
             raise RuntimeError("Compile must be ran before running any iterations")
         call = self._next_call()
         if self._kind == "device":
+            self._apply_shape()
             n = self.n_events
             if self._uniform_source is None:
                 self._sample(n, 0, call, self._int_id, self._params_dev, train, False)
@@ -459,15 +466,44 @@ class MonteCarloFlow(ABC):
         if self.device.type == "cuda":
             self._choose_rows()
             self._ws.clear()
+            if self._autotune:
+                self.tune_launch()
         if trace:
             self.trace(n_events=23)
 
     def _compile_cuda_integrand(self, integrand):
         return integrand.compile_for(self._ALG, self._prec, self.n_dim)
 
+    # ---------------------------------------------------------------- launch shape
+    @property
+    def launch_shape(self):
+        """The fp32 sampler launch shape this integrator uses (``None`` = default)."""
+        return self._shape
+
+    def set_launch_shape(self, shape):
+        """Use ``shape`` (an ``autotune.LaunchShape`` or ``None`` for the default)
+        for this integrator's fused fp32 sampler launches."""
+        self._shape = shape
+        if self.device.type == "cuda" and self.event is not None:
+            self._choose_rows()
+
+    def tune_launch(self, force=False):
+        """Time the candidate launch shapes on this workload (or read the cached
+        winner) and use the fastest; returns it, or ``None`` where the
+        configuration has no launch shape to choose (not fused fp32 VEGAS)."""
+        shape = autotune.tune(self, force=force)
+        if shape is not None:
+            self.set_launch_shape(shape)
+        return shape
+
+    def _apply_shape(self):
+        if autotune.fused_f32(self):
+            autotune.ensure(self._shape or autotune.DEFAULT_SHAPE)
+
     def _choose_rows(self):
         lib = nat.load()
         import ctypes
+        self._apply_shape()
         rows = ctypes.c_int(0)
         integ = self._int_id if self._kind == "device" else nat.VF_INT_SYMGAUSS
         nat.check(lib.vf_sample_rows(self._ALG, self._prec, self.n_dim, integ, 1, ctypes.byref(rows)))

@@ -26,6 +26,7 @@ class VegasFlow(MonteCarloFlow):
     """Importance sampling (vflow.py:215)."""
 
     _ALG = nat.VF_ALG_VEGAS
+    _FUSED_F32_SAMPLER = True
 
     def __init__(self, n_dim, n_events, train=True, main_dimension=0, **kwargs):
         super().__init__(n_dim, n_events, **kwargs)

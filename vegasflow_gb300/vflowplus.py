@@ -46,6 +46,8 @@ def stratification(n_dim, n_events, adaptive):
 class VegasFlowPlus(VegasFlow):
     """VEGAS+ (vflowplus.py:83)."""
 
+    _FUSED_F32_SAMPLER = False  # samples per hypercube through its own kernels
+
     def __init__(self, n_dim, n_events, train=True, adaptive=False, events_limit=None, **kwargs):
         if events_limit is None:  # vflowplus.py:89-99
             logger.info("Events per device limit set to %d", n_events)
