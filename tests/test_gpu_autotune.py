@@ -81,3 +81,32 @@ def test_autotune_is_noop_off_the_fused_path(tmp_path, monkeypatch):
     inst.compile(integrands.symgauss())
     assert inst.launch_shape is None
     assert not (tmp_path / "s.json").exists()
+
+
+def _hist(inst):
+    """One sampling pass on the current grid (always the same Philox call, so
+    the same events); the (n_dim, 50) arr_res2 it fills."""
+    inst._call_ctr = 1000
+    inst._fill_partials(train=True)
+    inst._end_iteration(train=False, want_hist=True)
+    return inst._workspace()["hist"].cpu().numpy().copy()
+
+
+@pytest.mark.parametrize("n_dim", [3, 8, 12, 16])
+@pytest.mark.parametrize("trained", [False, True])
+def test_hist_layouts_agree(n_dim, trained):
+    """Every histogram layout fills the same per-bin sums (to float rounding and,
+    for the fixed-point tables, the dither) on the same events and grid."""
+    inst = VegasFlow(n_dim, 1_000_000, precision="fp32", seed=4, verbose=False)
+    inst.compile(integrands.symgauss(0.2))
+    if trained:
+        inst.run_integration(4)
+    hists = {}
+    for layout in (0, 4, 8):
+        inst.set_launch_shape(autotune.LaunchShape(256, 0, layout))
+        hists[layout] = _hist(inst)
+    ref = hists[0]
+    assert np.all(np.isfinite(ref)) and ref.sum() > 0
+    for layout, h in hists.items():
+        scale = ref.sum(axis=1, keepdims=True)
+        np.testing.assert_allclose(h / scale, ref / scale, rtol=0, atol=2e-4, err_msg=f"layout {layout}")

@@ -8,7 +8,8 @@ beyond float rounding (the Philox stream is indexed by event, not by thread):
   block size it fixes how many events each thread walks, and the number of
   partial rows the iteration-end kernel reduces;
 * ``hist_copies``   -- histogram layout while training: 0 = joint tables of
-  dimension pairs, 1|2|4 = per-dimension tables with that many copies per warp.
+  dimension pairs, 1|2|4 = per-dimension tables with that many copies per warp,
+  8 = the joint tables in fixed point (integer atomics).
 
 ``tune()`` times every candidate on the integrator's own workload (grid,
 integrand, event count) with CUDA events on the launching stream, keeps the
@@ -31,7 +32,7 @@ import torch
 
 from . import _native as nat
 
-HIST_CANDIDATES = (0, 4, 2)
+HIST_CANDIDATES = (0, 8, 4)
 THREAD_CANDIDATES = (256, 128)
 BLOCKS_PER_SM_CANDIDATES = (0, 2, 1)
 
@@ -48,8 +49,8 @@ class LaunchShape:
             raise ValueError(f"threads must be 128 or 256, not {threads}")
         if not 0 <= blocks_per_sm <= 16:
             raise ValueError(f"blocks_per_sm must be in 0..16, not {blocks_per_sm}")
-        if hist_copies not in (0, 1, 2, 4):
-            raise ValueError(f"hist_copies must be 0, 1, 2 or 4, not {hist_copies}")
+        if hist_copies not in (0, 1, 2, 4, 8):
+            raise ValueError(f"hist_copies must be 0, 1, 2, 4 or 8, not {hist_copies}")
         self.threads = int(threads)
         self.blocks_per_sm = int(blocks_per_sm)
         self.hist_copies = int(hist_copies)

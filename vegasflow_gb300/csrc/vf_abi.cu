@@ -110,8 +110,8 @@ int vf_tune_set(int key, int value) {
     return VF_OK;
   }
   if (key == VF_TUNE_F32_HIST_COPIES) {
-    if (value != 0 && value != 1 && value != 2 && value != 4)
-      return fail(VF_ERR_ARG, "vf_tune_set: histogram layout must be 0 (joint pairs) or 1, 2, 4");
+    if (value != 0 && value != 1 && value != 2 && value != 4 && value != VF_F32_HIST_FIXED)
+      return fail(VF_ERR_ARG, "vf_tune_set: histogram layout must be 0 (joint pairs), 1, 2, 4 or 8 (fixed point)");
     g_f32_hist_copies.store(value);
     return VF_OK;
   }
@@ -319,8 +319,8 @@ int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int
   a.n_out = n_out;
   a.train = train ? 1 : 0;
   a.iter = iter;
-  const int blocks = (a.train || hist_out) ? n_dim + 1 : 1;
-  vf::vf_iteration_end_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(a);
+  const int clusters = (a.train || hist_out) ? n_dim + 1 : 1;
+  vf::vf_iteration_end_kernel<<<clusters * VF_END_CLUSTER, VF_END_THREADS, 0, (cudaStream_t)stream>>>(a);
   return check_launch("vf_iteration_end");
 }
 

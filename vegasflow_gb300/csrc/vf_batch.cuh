@@ -265,19 +265,13 @@ __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a)
   const int item = a.blk_item[blockIdx.x];
   const int role = a.blk_role[blockIdx.x];
   const BatchItem it = a.items[item];
-  __shared__ double part[4][64];
   __shared__ double hsm[VF_BINS];
   __shared__ double red[2][256];
   if (role >= 0) {
     if (!it.train) return;
-    const int c = t & 63, r0 = t >> 6;
-    double s = 0.0;
-    if (c < VF_BINS)
-      for (int k = r0; k < it.n_tiles; k += 4) s += a.partials[a.tile_row[it.tile0 + k] + 2 + role * VF_BINS + c];
-    part[r0][c] = s;
-    __syncthreads();
-    if (t < VF_BINS) hsm[t] = ((part[0][t] + part[1][t]) + part[2][t]) + part[3][t];
-    __syncthreads();
+    const double* partials = a.partials + 2 + role * VF_BINS;
+    const long long* rows = a.tile_row + it.tile0;
+    sum_hist_columns<5>([=](int k) { return partials + rows[k]; }, it.n_tiles, hsm, nullptr);
     refine_dimension(hsm, a.grids + it.grid_off + role * VF_EDGES, a.alpha, a.flags);
     return;
   }

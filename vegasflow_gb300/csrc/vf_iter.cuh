@@ -6,6 +6,8 @@
 #include "vf_device.cuh"
 #include "vf_refine.cuh"
 
+#include <cooperative_groups.h>
+
 namespace vf {
 
 struct IterEndArgs {
@@ -25,53 +27,73 @@ struct IterEndArgs {
   int iter;
 };
 
-// Block d < D (when train or hist_out): histogram of dimension d, then refine
-// it when train.  The last block: res/res2, sigma, history, average.
-__global__ void __launch_bounds__(256) vf_iteration_end_kernel(const IterEndArgs a) {
+// The iteration-end kernel runs in clusters of VF_END_CLUSTER blocks: cluster
+// d < D reduces dimension d's histogram columns, each block over 1/8 of the
+// partial rows (the float64 additions spread over 8 SMs), and block 0 of the
+// cluster adds the 8 block sums in rank order through distributed shared
+// memory and refines the grid row.  The last cluster's block 0 does the
+// integral sums.  Every sum has a fixed order, so the result does not depend
+// on scheduling.
+#define VF_END_CLUSTER 8
+#define VF_END_THREADS 512
+#define VF_END_LANES 10
+
+__global__ void __cluster_dims__(VF_END_CLUSTER, 1, 1) __launch_bounds__(VF_END_THREADS)
+vf_iteration_end_kernel(const IterEndArgs a) {
+  namespace cg = cooperative_groups;
+  const cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int group = blockIdx.x / VF_END_CLUSTER;
   const int t = threadIdx.x;
   const int D = a.n_dim;
   const int K = a.n_out;
-  const int W = 2 * K + VF_BINS * D;
-  __shared__ double part[4][64];
+  const long long W = 2 * K + VF_BINS * D;
+  __shared__ double mine[VF_BINS];
   __shared__ double hsm[VF_BINS];
   const bool per_dim = a.train || a.hist_out != nullptr;
-  if (per_dim && (int)blockIdx.x < D) {
-    const int d = blockIdx.x;
-    const int c = t & 63, r0 = t >> 6;  // 4 row lanes x 64 columns
-    double s = 0.0;
-    if (c < VF_BINS)
-      for (int r = r0; r < a.rows; r += 4) s += a.partials[(long long)r * W + 2 * K + d * VF_BINS + c];
-    part[r0][c] = s;
-    __syncthreads();
-    if (t < VF_BINS) {
-      const double v = ((part[0][t] + part[1][t]) + part[2][t]) + part[3][t];
+  if (per_dim && group < D) {
+    const int d = group;
+    const int lo = (int)((long long)a.rows * rank / VF_END_CLUSTER);
+    const int hi = (int)((long long)a.rows * (rank + 1) / VF_END_CLUSTER);
+    const double* col0 = a.partials + 2 * K + d * VF_BINS + lo * W;
+    sum_hist_columns<VF_END_LANES>([=](int r) { return col0 + r * W; }, hi - lo, mine, nullptr);
+    cluster.sync();
+    if (rank == 0 && t < VF_BINS) {
+      double v = mine[t];
+      for (int r = 1; r < VF_END_CLUSTER; ++r) v += cluster.map_shared_rank(mine, r)[t];
       hsm[t] = v;
       if (a.hist_out) a.hist_out[d * VF_BINS + t] = v;
     }
-    __syncthreads();
-    if (a.train) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
+    cluster.sync();  // the other blocks keep their shared memory until block 0 has read it
+    if (rank == 0 && a.train) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
     return;
   }
+  if (rank != 0) return;
   // ---- the sums, one output at a time
-  __shared__ double red[2][256];
+  __shared__ double red[2][VF_END_THREADS / 32];
+  const int lane = t & 31, warp = t >> 5;
   for (int j = 0; j < K; ++j) {
     double s1 = 0.0, s2 = 0.0;
     for (int r = t; r < a.rows; r += blockDim.x) {
       s1 += a.partials[(long long)r * W + j];
       s2 += a.partials[(long long)r * W + K + j];
     }
-    red[0][t] = s1;
-    red[1][t] = s2;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (t < o) {
-        red[0][t] += red[0][t + o];
-        red[1][t] += red[1][t + o];
-      }
-      __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     }
+    if (lane == 0) {
+      red[0][warp] = s1;
+      red[1][warp] = s2;
+    }
+    __syncthreads();
     if (t == 0) {
-      const double res = red[0][0], res2 = red[1][0];
+      double res = 0.0, res2 = 0.0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+        res += red[0][i];
+        res2 += red[1][i];
+      }
       const double N = a.n_events;
       // vflow.py:437-438 (and plain.py:37-43, the same expression)
       const double err_tmp2 = __ddiv_rn(__dsub_rn(__dmul_rn(N, res2), __dmul_rn(res, res)), __dsub_rn(N, 1.0));

@@ -290,22 +290,12 @@ __global__ void __launch_bounds__(256) vf_plus_iteration_end_kernel(const PlusEn
   const int D = a.n_dim;
   const int H = a.n_hcubes;
   const int W = 2 + VF_BINS * D;
-  __shared__ double part[4][64];
   __shared__ double hsm[VF_BINS];
   if ((a.train || a.hist_out) && (int)blockIdx.x < D) {
     const int d = blockIdx.x;
-    const int c = t & 63, r0 = t >> 6;
-    double s = 0.0;
-    if (c < VF_BINS)
-      for (int r = r0; r < a.rows; r += 4) s += a.partials[(long long)r * W + 2 + d * VF_BINS + c];
-    part[r0][c] = s;
-    __syncthreads();
-    if (t < VF_BINS) {
-      const double v = ((part[0][t] + part[1][t]) + part[2][t]) + part[3][t];
-      hsm[t] = v;
-      if (a.hist_out) a.hist_out[d * VF_BINS + t] = v;
-    }
-    __syncthreads();
+    const double* col0 = a.partials + 2 + d * VF_BINS;
+    sum_hist_columns<5>([=](int r) { return col0 + (long long)r * W; }, a.rows, hsm,
+                        a.hist_out ? a.hist_out + d * VF_BINS : nullptr);
     if (a.train) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
     return;
   }

@@ -17,8 +17,9 @@
 //   applied in float64 to the block partials.
 //
 // Per event: accumulation of w f and (w f)^2 in TwoSum-compensated fp32, and
-// (when training) the (w f)^2 histogram in shared memory, in one of two layouts
-// (`hist_copies`):
+// (when training) the (w f)^2 histogram in shared memory, in one of three
+// layouts (`hist_copies`; which is fastest depends on the dimension count and
+// the spread of the weights, so the launch-shape autotuner chooses):
 //   0      joint pairs (the default): dimensions (0,1), (2,3), ... share one
 //          50 x 50 table per block, so an event makes ceil(D/2) float atomic
 //          additions instead of D, and with 2500 cells the lanes of a warp rarely
@@ -26,6 +27,18 @@
 //          row or column sums of its pair's table (an odd last dimension keeps a
 //          plain 50-bin table).
 //   1,2,4  per-dimension tables, that many copies per warp (lane groups).
+//   8      fixed point (VF_F32_HIST_FIXED): the joint pair tables of layout 0
+//          as 32-bit integers, updated with native integer shared atomics (no
+//          result read back) instead of float atomics, which the hardware runs
+//          as compare-and-swap loops.  An event adds q = floor(S (w f)^2 + r),
+//          r a per-event dither in [0, 1) (a Weyl sequence of the event number),
+//          so the expectation of q / S is exact.  A cell cannot wrap: q is
+//          capped at Qmax = (2^32 - 1) / (events the block walks), and an event
+//          at or above the cap goes to a per-dimension float table instead.
+//          Each block picks its power-of-two scale S from the first event of
+//          every thread (S (w f)^2 about Qmax / 512 at their geometric mean);
+//          a block whose first events are all zero uses the float table only.
+//          The integer sums do not depend on the order of the atomics.
 #pragma once
 #include "vf_sample.cuh"
 
@@ -43,11 +56,19 @@ __device__ __forceinline__ float ex2_approx_ftz(float x) {
 
 __host__ __device__ inline int vegas_f32_joint_floats(int D) { return (D / 2) * 2500 + (D & 1) * 50; }
 
+// the fixed-point histogram layout (hist_copies value)
+#define VF_F32_HIST_FIXED 8
+
 __host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, int train,
                                                     int threads = VF_THREADS) {
   const int nb = D * VF_BINS;
-  const int hist = copies_per_warp == 0 ? vegas_f32_joint_floats(D) * 4
-                                        : (threads / 32) * copies_per_warp * nb * 4;
+  int hist;
+  if (copies_per_warp == 0)
+    hist = vegas_f32_joint_floats(D) * 4;
+  else if (copies_per_warp == VF_F32_HIST_FIXED)
+    hist = (vegas_f32_joint_floats(D) + nb) * 4;  // integer joint tables, float overflow table
+  else
+    hist = (threads / 32) * copies_per_warp * nb * 4;
   return nb * 8 + (train ? hist : 0);
 }
 
@@ -68,6 +89,10 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   const bool train = a.train != 0;
   const bool limits = a.xmin != nullptr;
   const int cpw = a.hist_copies;
+  const bool fixedp = train && cpw == VF_F32_HIST_FIXED;
+  // fixed-point layout: integer joint tables (as layout 0), float overflow table [NB]
+  u32* hint = reinterpret_cast<u32*>(hist);
+  float* hovf = reinterpret_cast<float*>(hint + vegas_f32_joint_floats(D));
 
   // ---- per-block float64 constants: Gaussian centres and k_d = sqrt(log2 e)/a_d,
   // and the weight constant 50^D * xjac (* pref / prod k_d)
@@ -108,6 +133,8 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   if (train) {
     if (cpw == 0)
       for (int k = tid; k < NP * 2500 + (D & 1) * VF_BINS; k += blockDim.x) hist[k] = 0.0f;
+    else if (fixedp)
+      for (int k = tid; k < vegas_f32_joint_floats(D) + NB; k += blockDim.x) hint[k] = 0u;  // 0 and 0.0f
     else
       for (int k = tid; k < (THREADS / 32) * cpw * NB; k += blockDim.x) hist[k] = 0.0f;
   }
@@ -121,10 +148,32 @@ vf_vegas_f32_kernel(const SampleArgs a) {
   if (!GAUSS) load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
 
   float* my_hist = hist + (warp * cpw + ((lane * cpw) >> 5)) * NB;
+  float hscale = 1.0f;  // fixed point: the block's power-of-two scale S
+  float qcap = 0.0f;    // fixed point: Qmax (0: the float table only)
   F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
 
-  // one event from its per-dimension (bin, m) pairs
-  auto finish = [&](const int (&bins)[D], float wf, float s, const float (&x)[D]) {
+  // fixed point: add (w f)^2 of event `ev` to its D bins
+  auto add_fixed = [&](const int (&bins)[D], float v2, u64 ev) {
+    const float r = (float)((u32)ev * 0x9E3779B9u) * 2.3283064e-10f;  // Weyl dither in [0, 1)
+    const float q = fmaf(v2, hscale, r);
+    if (q < qcap) {
+      const u32 qi = __float2uint_rd(q);
+      if (qi != 0u) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p)
+          atomicAdd(hint + p * 2500 + (bins[2 * p] - 2 * p * VF_BINS) * VF_BINS +
+                        (bins[2 * p + 1] - (2 * p + 1) * VF_BINS),
+                    qi);
+        if (D & 1) atomicAdd(hint + NP * 2500 + (bins[D - 1] - (D - 1) * VF_BINS), qi);
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) atomicAdd(hovf + bins[d], v2);
+    }
+  };
+
+  // one event from its per-dimension (bin, m) pairs; returns (w f)^2
+  auto finish = [&](const int (&bins)[D], float wf, float s, const float (&x)[D]) -> float {
     float f;
     if constexpr (GAUSS) {
       f = ex2_approx_ftz(-s);
@@ -140,7 +189,7 @@ vf_vegas_f32_kernel(const SampleArgs a) {
     const float v2 = v * v;
     two_sum_add(s1, v);
     two_sum_add(s2, v2);
-    if (train) {
+    if (train && !fixedp) {
       if (cpw == 0) {
 #pragma unroll
         for (int p = 0; p < NP; ++p)
@@ -153,41 +202,93 @@ vf_vegas_f32_kernel(const SampleArgs a) {
         for (int d = 0; d < D; ++d) atomicAdd(my_hist + bins[d], v2);
       }
     }
+    return v2;
+  };
+
+  // one event's Philox words -> bins, weight and the Gaussian exponent (or x)
+  auto draw = [&](u64 ev, int (&bins)[D], float& wf, float& s, float (&x)[D]) {
+#pragma unroll
+    for (int q = 0; q < (D + 3) / 4; ++q) {
+      u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+      philox4x32_10_rk(c0, c1, c2, c3, a.rk);
+      const u32 wq[4] = {c0, c1, c2, c3};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int d = 4 * q + j;
+        if (d < D) {
+          const u64 pp = (u64)(~wq[j]) * 50ull + 25ull;
+          const int i = (int)(pp >> 32);
+          const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
+          const float2 c = cells[d * VF_BINS + i];
+          const float t = fmaf(c.y, m, c.x);
+          wf = (d == 0) ? c.y : wf * c.y;
+          if (GAUSS)
+            s = fmaf(t, t, s);
+          else
+            x[d] = t;
+          bins[d] = d * VF_BINS + i;
+        }
+      }
+    }
   };
 
   const long long n = a.n_events;
   const long long stride = (long long)gridDim.x * blockDim.x;
   long long e = (long long)blockIdx.x * blockDim.x + tid;
   if (a.u_inj == nullptr) {
+    if (fixedp) {
+      // Qmax from the most events the block walks, and the block's scale from
+      // the first event of every thread: S = 2^k, k = floor(log2 Qmax) - 9 -
+      // round(mean log2 (w f)^2) over the normal finite values
+      __shared__ float lsum[THREADS / 32];
+      __shared__ int lcnt[THREADS / 32];
+      int bins[D];
+      float x[D];
+      float wf = 1.0f, s = 0.0f, v2 = 0.0f;
+      const u64 ev = (u64)(a.ev_offset + e);
+      const bool have = e < n;
+      if (have) {
+        draw(ev, bins, wf, s, x);
+        v2 = finish(bins, wf, s, x);
+      }
+      const bool use = have && v2 >= 1.17549435e-38f && v2 <= 3.40282347e38f;  // normal, finite
+      float l = use ? __log2f(v2) : 0.0f;
+      int c = use ? 1 : 0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+      }
+      if (lane == 0) {
+        lsum[warp] = l;
+        lcnt[warp] = c;
+      }
+      __syncthreads();
+      float ls = 0.0f;
+      int cs = 0;
+#pragma unroll
+      for (int i = 0; i < THREADS / 32; ++i) {
+        ls += lsum[i];
+        cs += lcnt[i];
+      }
+      const long long per_thread = n > 0 ? (n + stride - 1) / stride : 1;
+      const float cap = floorf((float)(4294967295.0 / ((double)THREADS * (double)per_thread)));
+      const int cap_log2 = (int)((__float_as_uint(cap) >> 23) & 0xFF) - 127;  // floor(log2 Qmax)
+      int k = cap_log2 - 9 - (cs > 0 ? __float2int_rn(ls / (float)cs) : 0);
+      k = k < -126 ? -126 : (k > 127 ? 127 : k);
+      hscale = __int_as_float((127 + k) << 23);  // 2^k
+      qcap = cs > 0 ? cap : 0.0f;
+      if (have) add_fixed(bins, v2, ev);
+      e += stride;
+    }
     for (; e < n; e += stride) {
       const u64 ev = (u64)(a.ev_offset + e);
       int bins[D];
       float x[D];
       float wf = 1.0f, s = 0.0f;
-#pragma unroll
-      for (int q = 0; q < (D + 3) / 4; ++q) {
-        u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
-        philox4x32_10_rk(c0, c1, c2, c3, a.rk);
-        const u32 wq[4] = {c0, c1, c2, c3};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int d = 4 * q + j;
-          if (d < D) {
-            const u64 pp = (u64)(~wq[j]) * 50ull + 25ull;
-            const int i = (int)(pp >> 32);
-            const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
-            const float2 c = cells[d * VF_BINS + i];
-            const float t = fmaf(c.y, m, c.x);
-            wf = (d == 0) ? c.y : wf * c.y;
-            if (GAUSS)
-              s = fmaf(t, t, s);
-            else
-              x[d] = t;
-            bins[d] = d * VF_BINS + i;
-          }
-        }
-      }
-      finish(bins, wf, s, x);
+      draw(ev, bins, wf, s, x);
+      const float v2 = finish(bins, wf, s, x);
+      if (fixedp) add_fixed(bins, v2, ev);
     }
   } else {
     int bad = 0;
@@ -215,7 +316,9 @@ vf_vegas_f32_kernel(const SampleArgs a) {
           x[d] = t;
         bins[d] = d * VF_BINS + i;
       }
-      finish(bins, wf, s, x);
+      const float v2 = finish(bins, wf, s, x);
+      if (fixedp)  // injected uniforms (a checking path): the float table, no scale
+        for (int d = 0; d < D; ++d) atomicAdd(hovf + bins[d], v2);
     }
     if (bad && a.flags) atomicOr(a.flags, VF_FLAG_INDEX_RANGE);
   }
@@ -265,6 +368,25 @@ vf_vegas_f32_kernel(const SampleArgs a) {
         } else {
           hf = hist[NP * 2500 + b];
         }
+      } else if (fixedp) {
+        const int d = k / VF_BINS, b = k - d * VF_BINS;
+        u64 total = 0;
+        if (d < 2 * NP) {
+          const u32* tab = hint + (d >> 1) * 2500;
+          if ((d & 1) == 0)
+            for (int c = 0; c < VF_BINS; ++c) total += tab[b * VF_BINS + c];  // row sum
+          else
+            for (int r = 0; r < VF_BINS; ++r) total += tab[r * VF_BINS + b];  // column sum
+        } else {
+          total = hint[NP * 2500 + b];
+        }
+        hf = hovf[k];
+        const double h = ((double)total / (double)hscale + (double)hf) * s2c;
+        if (a.accumulate)
+          row[2 + k] += h;
+        else
+          row[2 + k] = h;
+        continue;
       } else {
         for (int c = 0; c < ncopies; ++c) hf += hist[c * NB + k];
       }
