@@ -34,6 +34,8 @@ extern "C" {
 #define VF_FLAG_INDEX_RANGE 1     /* a uniform mapped outside the grid (clamped)  */
 #define VF_FLAG_REFINE_OVERRUN 2  /* the rebinning walk ran past the last bin     */
 #define VF_FLAG_NONFINITE 4       /* a partial sum was NaN or Inf                 */
+#define VF_FLAG_TIMEOUT 8         /* a bounded device-side wait gave up (a copy that
+                                     never completed); that launch's sums are partial */
 
 /* ---- constants (configflow.py:13-24) -------------------------------------- */
 #define VF_BINS_MAX 50

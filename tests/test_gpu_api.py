@@ -45,6 +45,9 @@ def instance_and_compile(Integrator, mode=0, integrand_function=example_integran
     elif mode == 3:
         def integrand(xarr, n_dim=None, weight=None):
             return integrand_function(xarr, weight=None)
+    # seeded so the suite is reproducible (the reference's tests draw a fresh
+    # seed every run, so their 3-sigma checks fail now and then)
+    kw.setdefault("seed", 1000 + mode)
     int_instance = Integrator(dim, ncalls, verbose=False, **kw)
     int_instance.compile(integrand)
     return int_instance
@@ -68,7 +71,7 @@ def test_VegasFlow(mode):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_VegasFlow_device_integrand(precision):
-    inst = VegasFlow(dim, ncalls, verbose=False, precision=precision)
+    inst = VegasFlow(dim, ncalls, verbose=False, precision=precision, seed=7)
     inst.compile(integrands.symgauss())
     _ = inst.run_integration(n_iter)
     inst.freeze_grid()

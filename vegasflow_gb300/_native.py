@@ -26,6 +26,7 @@ VF_ERR_UNSUPPORTED = 7
 VF_FLAG_INDEX_RANGE = 1
 VF_FLAG_REFINE_OVERRUN = 2
 VF_FLAG_NONFINITE = 4
+VF_FLAG_TIMEOUT = 8
 
 VF_ALG_VEGAS = 0
 VF_ALG_PLAIN = 1

@@ -1,5 +1,7 @@
 // The extern "C" entry points of libvegasgb.so (declared in
 // include/vegasflow_gb300.h): argument checks, kernel selection, launch.
+#include <cuda.h>
+
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -62,6 +64,50 @@ bool evaluating_builtin(int id) { return id >= VF_INT_SYMGAUSS && id <= VF_INT_S
 // The specialised fp32 VEGAS kernel serves evaluating launches without taps.
 bool use_vegas_f32(int alg, int precision, int integrand, bool taps) {
   return precision == VF_PREC_F32 && alg == VF_ALG_VEGAS && evaluating_builtin(integrand) && !taps;
+}
+
+// cuTensorMapEncodeTiled, resolved through the runtime (the library does not
+// link the driver library).
+typedef CUresult (*PfnTensorMapEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                            const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                            CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                            CUtensorMapFloatOOBfill);
+
+PfnTensorMapEncodeTiled tensor_map_encoder() {
+  static PfnTensorMapEncodeTiled fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PfnTensorMapEncodeTiled>(p);
+  }();
+  return fn;
+}
+
+// The tensor map of injected uniforms [n][D] float64 with a box of `threads`
+// rows, for D in {4, 8, 16} (rows of 32/64/128 bytes, swizzled by as many);
+// returns the swizzle code (1|2|3) or 0 where the plain-load path applies.
+int encode_uniform_tiles(vf::SampleArgs& a, const double* u, long long n, int D, int threads) {
+  static_assert(sizeof(CUtensorMap) == sizeof(a.tmap), "tensor map size");
+  const int code = D == 4 ? 1 : D == 8 ? 2 : D == 16 ? 3 : 0;
+  if (!code || !u || (reinterpret_cast<size_t>(u) & 15) != 0 || n < 1 || n > (1ll << 31) - 1024) return 0;
+  const PfnTensorMapEncodeTiled enc = tensor_map_encoder();
+  if (!enc) return 0;
+  const cuuint64_t dims[2] = {(cuuint64_t)D, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)D * 8};
+  const cuuint32_t box[2] = {(cuuint32_t)D, (cuuint32_t)threads};
+  const cuuint32_t elem[2] = {1, 1};
+  const CUtensorMapSwizzle swz = code == 1   ? CU_TENSOR_MAP_SWIZZLE_32B
+                                 : code == 2 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                             : CU_TENSOR_MAP_SWIZZLE_128B;
+  CUtensorMap* tm = reinterpret_cast<CUtensorMap*>(a.tmap);
+  if (enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(u), dims, strides, box, elem,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return 0;
+  return code;
 }
 
 void fill_philox(vf::SampleArgs& a, unsigned long long seed, unsigned int call) {
@@ -235,6 +281,8 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   a.alg = alg;
   a.train = train ? 1 : 0;
   a.accumulate = accumulate ? 1 : 0;
+  a.tma_swizzle = 0;
+  a.rows_total = rows;
   fill_philox(a, seed, call_ctr);
   if (jit) {
     if (taps && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS)
@@ -247,9 +295,26 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
     return rc ? rc : check_launch("vf_sample (JIT)");
   }
   int smem;
+  int blocks = rows;
   if (fast) {
     a.hist_copies = g_f32_hist_copies.load();
     smem = vf::vegas_f32_smem_bytes(n_dim, a.hist_copies, a.train, threads);
+    if (u_inj) {
+      // injected uniforms through TMA: one stage of `threads` rows, 1024-byte
+      // aligned; the grid is capped at the blocks that fit at once (the kernel
+      // clears the rows it does not own)
+      a.tma_swizzle = encode_uniform_tiles(a, u_inj, n_events, n_dim, threads);
+      if (a.tma_swizzle) {
+        smem += threads * 8 * n_dim + 1024;
+        int rc = prepare_smem(k, smem);
+        if (rc) return rc;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem) != cudaSuccess || per_sm < 1)
+          return fail(VF_ERR_CUDA, "vf_sample: occupancy query for the TMA path failed");
+        const int fit = per_sm * sm_count();
+        if (fit < blocks) blocks = fit;
+      }
+    }
   } else {
     a.hist_copies = hist_copies_for(precision);
     const int real = precision == VF_PREC_F64 ? 8 : 4;
@@ -259,7 +324,7 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   if (rc) return rc;
   void* args[] = {&a};
   const cudaError_t e =
-      cudaLaunchKernel(k, dim3(rows), dim3(threads), args, smem, (cudaStream_t)stream);
+      cudaLaunchKernel(k, dim3(blocks), dim3(threads), args, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "vf_sample launch: %s", cudaGetErrorString(e));
   return check_launch("vf_sample");
 }

@@ -22,6 +22,7 @@
 #define VF_FLAG_INDEX_RANGE 1  // an injected uniform mapped outside the grid (clamped)
 #define VF_FLAG_REFINE_OVERRUN 2  // the rebinning walk ran past the last bin
 #define VF_FLAG_NONFINITE 4    // a partial sum was NaN or Inf
+#define VF_FLAG_TIMEOUT 8      // a bounded wait gave up (a copy never completed)
 
 namespace vf {
 

@@ -50,6 +50,13 @@ struct SampleArgs {
   unsigned int ctr2[8];     // Philox counter word 2 of 4-word block q: (call << 4) | q;
                             // float64 uses ceil(D/2) <= 8 blocks, fp32 ceil(D/4) <= 4
   unsigned int ctr3;        // Philox counter word 3: call >> 28
+  // fp32 VEGAS kernel with injected uniforms: 0 = plain loads; 1|2|3 = tiles of
+  // THREADS events brought into shared memory by TMA through `tmap`, with the
+  // 32|64|128-byte swizzle (row bytes 8 D = 32|64|128)
+  int tma_swizzle;
+  int rows_total;           // partial rows the caller reduces; rows >= gridDim.x are cleared
+  // CUtensorMap of u_inj as a [n_events][D] float64 tensor, box [THREADS][D]
+  alignas(64) unsigned long long tmap[16];
 };
 
 // The 4 words of block q of event ev, with the host-computed keys/counters.

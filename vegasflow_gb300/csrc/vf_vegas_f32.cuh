@@ -56,6 +56,65 @@ __device__ __forceinline__ float ex2_approx_ftz(float x) {
 
 __host__ __device__ inline int vegas_f32_joint_floats(int D) { return (D / 2) * 2500 + (D & 1) * 50; }
 
+// The reference's bin of an injected float64 uniform u, ind = trunc(fl(50 *
+// fl(1 - u))) (vflow.py:117, :67), without float64 arithmetic: for u in
+// [2^-12, 1), U = u 2^64 is an exact 64-bit integer and y = 50 (1 - u) is
+// exactly (50 (2^64 - U)) / 2^64, an integer part and a 64-bit fraction.  The
+// reference's two roundings move y by less than 100 2^-53 < 2^-46, so
+// trunc(xn) = trunc(y) unless the fraction's top 32 bits are all zeros or all
+// ones (y within 2^-32 of an integer), where the caller repeats the float64
+// operations; so does every u outside [2^-12, 1) (and NaN, negative, >= 1).
+// m = 1 + the fraction's top 23 bits.  32-bit operations throughout: about 14
+// per uniform.  Returns false for the float64 cases.
+__device__ __forceinline__ bool inj_bin_exact(u64 bits, int& ind, float& m) {
+  const u32 bh = (u32)(bits >> 32), bl = (u32)bits;
+  const u32 sh = (bh >> 20) - 1011u;  // biased exponent - 1011: u in [2^-12, 1) <=> sh in [0, 11]
+  if (sh > 11u) return false;
+  const u32 mh = (bh & 0xFFFFFu) | 0x100000u;  // the mantissa's high word, implicit bit set
+  const u64 uu = ((u64)__funnelshift_l(bl, mh, sh) << 32) | (u64)(bl << sh);  // U = mantissa << sh
+  const u64 v = 0ull - uu;                                                      // 2^64 - U
+  const u64 p0 = (u64)(u32)v * 50ull;
+  const u64 p1 = (u64)(u32)(v >> 32) * 50ull + (p0 >> 32);  // 50 v = p1 2^32 + (u32)p0
+  const u32 fh = (u32)p1;                                    // the fraction's top 32 bits
+  if (fh + 1u < 2u) return false;
+  ind = (int)(p1 >> 32);
+  m = __uint_as_float((fh >> 9) | 0x3F800000u);
+  return true;
+}
+
+// ---- TMA staging of injected uniforms (tiles of THREADS events x D float64)
+__device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(u32 bar, u32 count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+// One tile: the barrier expects `bytes`, the tensor copy completes them.
+__device__ __forceinline__ void tma_load_tile(u32 dst, const void* tmap, int x, int y, u32 bar, u32 bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Wait for phase `parity` of the barrier, giving up after a bounded number of
+// polls (about a tenth of a second); returns whether the phase completed.
+__device__ __forceinline__ bool mbar_wait_bounded(u32 bar, u32 parity) {
+  for (int i = 0; i < (1 << 20); ++i) {
+    u32 ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (i >= 16) __nanosleep(64);
+  }
+  return false;
+}
+
 // the fixed-point histogram layout (hist_copies value)
 #define VF_F32_HIST_FIXED 8
 
@@ -76,7 +135,7 @@ __host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, 
 // (launch bounds) stays at 64 per thread for both.
 template <int D, int INTEG, int THREADS = VF_THREADS>
 __global__ void __launch_bounds__(THREADS, VF_F32_MIN_BLOCKS * VF_THREADS / THREADS)
-vf_vegas_f32_kernel(const SampleArgs a) {
+vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NB = D * VF_BINS;
   constexpr bool GAUSS = (INTEG == VF_INT_SYMGAUSS || INTEG == VF_INT_GAUSS);
@@ -291,22 +350,26 @@ vf_vegas_f32_kernel(const SampleArgs a) {
       if (fixedp) add_fixed(bins, v2, ev);
     }
   } else {
+    // injected float64 uniforms, [n][D] row-major, streamed once
     int bad = 0;
-    for (; e < n; e += stride) {
-      const double* up = a.u_inj + e * D;
+    auto injected_event = [&](const u64 (&ub)[D]) {
       int bins[D];
       float x[D];
       float wf = 1.0f, s = 0.0f;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        // the bin in float64, bit-exact with the reference (vflow.py:117, :67)
-        const double xn = __dmul_rn(50.0, __dsub_rn(1.0, up[d]));
-        int i = (int)xn;
-        if (i < 0 || i > VF_BINS - 1) {
-          bad = 1;
-          i = i < 0 ? 0 : VF_BINS - 1;
+        int i;
+        float m;
+        if (!inj_bin_exact(ub[d], i, m)) {
+          // the bin in float64, bit-exact with the reference (vflow.py:117, :67)
+          const double xn = __dmul_rn(50.0, __dsub_rn(1.0, __longlong_as_double((long long)ub[d])));
+          i = (int)xn;
+          if (i < 0 || i > VF_BINS - 1) {
+            bad = 1;
+            i = i < 0 ? 0 : VF_BINS - 1;
+          }
+          m = (float)(1.0 + (xn - floor(xn)));
         }
-        const float m = (float)(1.0 + (xn - floor(xn)));
         const float2 c = cells[d * VF_BINS + i];
         const float t = fmaf(c.y, m, c.x);
         wf = (d == 0) ? c.y : wf * c.y;
@@ -317,8 +380,75 @@ vf_vegas_f32_kernel(const SampleArgs a) {
         bins[d] = d * VF_BINS + i;
       }
       const float v2 = finish(bins, wf, s, x);
-      if (fixedp)  // injected uniforms (a checking path): the float table, no scale
+      if (fixedp)  // injected uniforms: the float table, no scale
         for (int d = 0; d < D; ++d) atomicAdd(hovf + bins[d], v2);
+    };
+    if (a.tma_swizzle != 0 && (D == 4 || D == 8 || D == 16)) {
+      // Tiles of THREADS events (the grid-stride assignment: tile t holds
+      // events t THREADS .. t THREADS + THREADS - 1, thread i takes event i)
+      // brought in by TMA into one shared-memory stage; the tensor map's
+      // swizzle (32/64/128 bytes for rows of 32/64/128 bytes) makes every
+      // quarter-warp read of a row conflict-free.  Each thread copies its row to
+      // registers, the block syncs, the next tile's copy is issued and then the
+      // events are evaluated, so the copy overlaps the arithmetic with a
+      // single 8 D THREADS-byte stage (registers are the second buffer).
+      constexpr int ROWB = 8 * D;
+      constexpr u32 TILEB = THREADS * ROWB;  // a multiple of 1024
+      __shared__ alignas(8) u64 tma_bar;
+      const u32 stage =
+          (smem_u32(smem) + (u32)vegas_f32_smem_bytes(D, cpw, a.train, THREADS) + 1023u) & ~1023u;
+      const u32 bar = smem_u32(&tma_bar);
+      const long long n_tiles = (n + THREADS - 1) / THREADS;
+      const long long G = gridDim.x;
+      if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (blockIdx.x < n_tiles) tma_load_tile(stage, a.tmap, 0, (int)(blockIdx.x * THREADS), bar, TILEB);
+      }
+      __syncthreads();
+      const u32 swz = (1u << a.tma_swizzle) - 1u;
+      u32 parity = 0;
+      for (long long t = blockIdx.x; t < n_tiles; t += G) {
+        const bool ok = mbar_wait_bounded(bar, parity);
+        parity ^= 1u;
+        if (!__syncthreads_and(ok)) {  // a copy never completed: report, stop
+          if (tid == 0 && a.flags) atomicOr(a.flags, VF_FLAG_TIMEOUT);
+          break;
+        }
+        u64 ub[D];
+#pragma unroll
+        for (int j = 0; j < D / 2; ++j) {
+          const u32 off = (u32)(tid * ROWB + 16 * j);
+          const u32 addr = stage + (off ^ (((off >> 7) & swz) << 4));
+          asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(ub[2 * j]), "=l"(ub[2 * j + 1]) : "r"(addr));
+        }
+        __syncthreads();  // the stage is read: refill it while the events are evaluated
+        if (tid == 0 && t + G < n_tiles) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          tma_load_tile(stage, a.tmap, 0, (int)((t + G) * THREADS), bar, TILEB);
+        }
+        if (t * THREADS + tid < n) injected_event(ub);
+      }
+    } else {
+      // plain loads: 16-byte (evict-first) when D is even and the array is
+      // 16-byte aligned
+      const bool vec = (D % 2 == 0) && ((reinterpret_cast<size_t>(a.u_inj) & 15) == 0);
+      for (; e < n; e += stride) {
+        const long long* up = reinterpret_cast<const long long*>(a.u_inj) + e * D;
+        u64 ub[D];
+        if (vec) {
+#pragma unroll
+          for (int j = 0; j < D / 2; ++j) {
+            const longlong2 v = __ldcs(reinterpret_cast<const longlong2*>(up) + j);
+            ub[2 * j] = (u64)v.x;
+            ub[2 * j + 1] = (u64)v.y;
+          }
+        } else {
+#pragma unroll
+          for (int d = 0; d < D; ++d) ub[d] = (u64)__ldcs(up + d);
+        }
+        injected_event(ub);
+      }
     }
     if (bad && a.flags) atomicOr(a.flags, VF_FLAG_INDEX_RANGE);
   }
@@ -397,6 +527,10 @@ vf_vegas_f32_kernel(const SampleArgs a) {
         row[2 + k] = h;
     }
   }
+  // rows beyond the grid (a launch with fewer blocks than the caller's rows)
+  if (!a.accumulate)
+    for (long long r = blockIdx.x + (long long)gridDim.x; r < a.rows_total; r += gridDim.x)
+      for (int k = tid; k < W; k += blockDim.x) a.partials[r * W + k] = 0.0;
 }
 
 }  // namespace vf

@@ -587,6 +587,9 @@ class MonteCarloFlow(ABC):
             logger.warning("a partial sum was NaN or Inf")
         if flags:
             self._workspace()["flags"].zero_()
+        if flags & nat.VF_FLAG_TIMEOUT:
+            raise nat.VegasGB300Error(nat.VF_ERR_TIMEOUT, "a device-side copy of injected uniforms never "
+                                      "completed; the iteration's sums are incomplete")
 
     def make_differentiable(self):
         raise NotImplementedError(
