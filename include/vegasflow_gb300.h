@@ -36,6 +36,8 @@ extern "C" {
 #define VF_FLAG_NONFINITE 4       /* a partial sum was NaN or Inf                 */
 #define VF_FLAG_TIMEOUT 8         /* a bounded device-side wait gave up (a copy that
                                      never completed); that launch's sums are partial */
+#define VF_FLAG_HISTORY_FULL 16   /* vf_iteration_dev found no history row left: that
+                                     iteration's result was not recorded              */
 
 /* ---- constants (configflow.py:13-24) -------------------------------------- */
 #define VF_BINS_MAX 50
@@ -120,12 +122,36 @@ int vf_reduce_events(int precision, const void* f, const void* w, const int* ind
  * (vflow.py:437-438), history[iter] = (res, sigma), the running
  * 1/sigma^2-weighted mean, its sigma and chi^2/dof in avg[n_out][5]
  * (monte_carlo.py:712-732), and -- when train -- refine_grid (vflow.py:349-362,
- * refine_grid_per_dimension vflow.py:135-211) on `grid` in place.
+ * refine_grid_per_dimension vflow.py:135-211) on `grid` in place: train = 1
+ * refines in float64 (the reference's default arithmetic), train = 2 in float32
+ * (the reference's float32 mode; what the fp32 sampler's grids use).
  */
 int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int train,
                      double n_events, double alpha, double* grid, double* hist_out,
                      double* sums_out, double* history, double* avg, int iter, int* flags,
                      void* stream);
+
+/*
+ * One whole iteration -- vf_sample over all n_events with a device integrand,
+ * then vf_iteration_end -- whose per-iteration values live in device memory, so
+ * that a CUDA graph captured around one call replays any number of iterations
+ * with no host work: *call_dev is the Philox call counter the sampler reads,
+ * *iter_dev the history row; the iteration end writes history[*iter_dev],
+ * updates avg, refines `grid` when train (VEGAS only), then advances both
+ * counters by one.  history has hist_cap rows of (res, sigma); an iteration that
+ * finds none left records nothing and sets VF_FLAG_HISTORY_FULL.  The same
+ * arithmetic as one _run_iteration of VegasFlow / PlainFlow
+ * (vflow.py:432-442, plain.py:18-43, monte_carlo.py:645-741); the reference
+ * has no device-side counterpart (TensorFlow traces its loop on the host).
+ * Launch sizes and shared-memory limits are set by the first (uncaptured)
+ * call for a configuration; a captured call makes no host-side CUDA call other
+ * than the two launches.
+ */
+int vf_iteration_dev(int alg, int precision, double* grid, int n_dim, long long n_events, double xjac,
+                     const double* xmin, const double* xdelta, double xdeltajac, unsigned long long seed,
+                     unsigned int* call_dev, int* iter_dev, int integrand, const double* params, int train,
+                     double alpha, double* partials, int rows, double* history, int hist_cap, double* avg,
+                     int* flags, void* stream);
 
 /*
  * VEGAS+ (VegasFlowPlus, vflowplus.py:83-247).  The events of an iteration are
@@ -264,6 +290,15 @@ int vf_jit_integrand(const char* source, const char* func_name, int alg, int pre
 /* Compile only (no GPU needed): VF_OK, or VF_ERR_JIT with the NVRTC log in `log`. */
 int vf_jit_check(const char* source, const char* func_name, int alg, int precision, int n_dim, char* log,
                  int log_size);
+
+/*
+ * Load every kernel of the library on the current device now (no counterpart
+ * in the reference).  Kernels are otherwise loaded at their first launch; on
+ * this platform a kernel loaded after a CUDA graph had been captured in the
+ * process took ~2 s to load, so code that captures graphs calls this first.
+ * Idempotent per device.
+ */
+int vf_preload(void);
 
 /*
  * Process-wide tunables picked by the autotuner (no counterpart in the

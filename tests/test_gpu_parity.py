@@ -270,3 +270,31 @@ def test_abi_rejects_bad_arguments():
     rc = lib.vf_sample(0, 0, None, 17, 10, 0, 0.1, None, None, 1.0, None, 1, 0, 1, None, 1, 0, None, 1,
                        None, None, None, None, None, None)
     assert rc == nat.VF_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("spread", [1.0, 4.0])
+def test_float32_refinement_close_to_float64(spread):
+    """vf_iteration_end with train=2 (the fp32 form's float32 refinement) moves
+    the edges to within float32 rounding of the float64 refinement (train=1),
+    keeps them ordered, and keeps the end points."""
+    rng = np.random.default_rng(int(spread))
+    n_dim = 6
+    hist = np.exp(spread * rng.standard_normal((n_dim, 50))) * 1e-3
+    row = np.concatenate([[1.0, 1.0], hist.reshape(-1)])
+    grid = np.sort(rng.random((n_dim, 51)), axis=1)
+    grid[:, 0], grid[:, -1] = 0.0, 1.0
+    lib = nat.load()
+    out = {}
+    for mode in (1, 2):
+        g = dev(grid)
+        part = dev(row)
+        history = torch.zeros(2, dtype=torch.float64, device="cuda")
+        avg = torch.zeros(5, dtype=torch.float64, device="cuda")
+        nat.check(lib.vf_iteration_end(nat.ptr(part), 1, n_dim, 1, mode, 1000.0, 1.5, nat.ptr(g), None, None,
+                                       nat.ptr(history), nat.ptr(avg), 0, None, nat.stream_handle()))
+        out[mode] = g.cpu().numpy()
+    want = np.stack([oracle.refine_grid_per_dimension(hist[d], grid[d]) for d in range(n_dim)])
+    np.testing.assert_allclose(out[1], want, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(out[2], want, rtol=0, atol=2e-5)
+    assert np.all(np.diff(out[2], axis=1) >= 0)
+    assert np.all(out[2][:, 0] == 0.0) and np.all(out[2][:, -1] == 1.0)

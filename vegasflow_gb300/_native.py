@@ -27,6 +27,7 @@ VF_FLAG_INDEX_RANGE = 1
 VF_FLAG_REFINE_OVERRUN = 2
 VF_FLAG_NONFINITE = 4
 VF_FLAG_TIMEOUT = 8
+VF_FLAG_HISTORY_FULL = 16
 
 VF_ALG_VEGAS = 0
 VF_ALG_PLAIN = 1
@@ -62,6 +63,8 @@ SIGNATURES = {
                   _P, _P, _P, _P, _P, _P],
     "vf_reduce_events": [_I, _P, _P, _P, _LL, _I, _I, _I, _I, _I, _P, _I, _P, _P],
     "vf_iteration_end": [_P, _I, _I, _I, _I, _D, _D, _P, _P, _P, _P, _P, _I, _P, _P],
+    "vf_iteration_dev": [_I, _I, _P, _I, _LL, _D, _P, _P, _D, _U64, _P, _P, _I, _P, _I, _D, _P, _I, _P, _I, _P,
+                         _P, _P],
     "vf_refine_grid": [_P, _P, _I, _D, _P, _P],
     "vf_consume_array_into_indices": [_P, _P, _LL, _I, _P, _P, _P],
     "vf_issue_probe": [_P, _I, _I, _P, _P],
@@ -77,6 +80,7 @@ SIGNATURES = {
     "vf_batch_iteration_end": [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P],
     "vf_jit_integrand": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, _P],
     "vf_jit_check": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, ctypes.c_char_p, _I],
+    "vf_preload": [],
     "vf_tune_set": [_I, _I],
     "vf_tune_get": [_I, _P],
 }

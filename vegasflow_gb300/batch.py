@@ -24,6 +24,7 @@ import torch
 from . import _native as nat
 from .configflow import BINS_MAX
 from .integrands import DeviceIntegrand
+from .utils import preload_kernels
 
 ITEM_DTYPE = np.dtype([("n_events", "<i8"), ("grid_off", "<i8"), ("param_off", "<i8"), ("xjac", "<f8"),
                        ("n_dim", "<i4"), ("integrand", "<i4"), ("stream_id", "<i4"), ("tile0", "<i4"),
@@ -51,6 +52,7 @@ class VegasBatch:
         if self.device.type != "cuda":
             raise RuntimeError("VegasBatch runs on a CUDA device only")
         nat.load()
+        preload_kernels(self.device)
         self.n_items = len(specs)
         self.seed = int.from_bytes(os.urandom(8), "little") & ((1 << 63) - 1) if seed is None else int(seed)
         self.tile_events = int(tile_events)

@@ -4,6 +4,8 @@
 
 #include <atomic>
 #include <cstdarg>
+#include <map>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 
@@ -122,13 +124,20 @@ void fill_philox(vf::SampleArgs& a, unsigned long long seed, unsigned int call) 
   a.ctr3 = call >> 28;
 }
 
+// Raise a kernel's dynamic shared-memory limit once per (device, kernel, size):
+// later launches (and launches inside a stream capture) make no attribute call.
 int prepare_smem(const void* kernel, int smem) {
-  if (smem > 48 * 1024) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess)
-      return fail(VF_ERR_CUDA, "cudaFuncSetAttribute(smem=%d): %s", smem, cudaGetErrorString(e));
-  }
+  if (smem <= 48 * 1024) return VF_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> done;
+  std::lock_guard<std::mutex> lock(mu);
+  int& have = done[{dev, kernel}];
+  if (have >= smem) return VF_OK;
+  const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return fail(VF_ERR_CUDA, "cudaFuncSetAttribute(smem=%d): %s", smem, cudaGetErrorString(e));
+  have = smem;
   return VF_OK;
 }
 
@@ -183,6 +192,45 @@ int vf_tune_get(int key, int* value) {
 
 const char* vf_last_error_string(void) { return g_err; }
 
+int vf_preload(void) {
+  // Lazily loaded kernels are loaded at their first launch; one loaded after a
+  // CUDA graph exists in the process was measured to stall ~2 s on this
+  // platform.  Loading them all here (a few hundred functions, once per device)
+  // keeps that out of later timed or captured work.
+  static std::mutex mu;
+  static bool done[128] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return fail(VF_ERR_CUDA, "vf_preload: no device");
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return VF_OK;
+  cudaFuncAttributes attr;
+  cudaError_t e = cudaSuccess;
+  auto load = [&](const void* k) {
+    if (k && e == cudaSuccess) e = cudaFuncGetAttributes(&attr, k);
+  };
+  for (int d = 1; d <= VF_MAX_DIM; ++d)
+    for (int integ = VF_INT_SYMGAUSS; integ <= VF_INT_SUM; ++integ) {
+      load(vf::vegas_f32_kernel(d, integ, 256));
+      load(vf::vegas_f32_kernel(d, integ, 128));
+    }
+  for (int dmax : {4, 8, 16})
+    for (int integ = VF_INT_NONE; integ <= VF_INT_SUM; ++integ) {
+      load(vf::sample_kernel_f64(dmax, integ));
+      load(vf::sample_kernel_f32(dmax, integ));
+    }
+  load((const void*)vf::vf_iteration_end_kernel);
+  load((const void*)vf::vf_refine_kernel);
+  load((const void*)vf::vf_consume_kernel);
+  load((const void*)vf::vf_reduce_events_kernel<double>);
+  load((const void*)vf::vf_reduce_events_kernel<float>);
+  if (e == cudaSuccess) e = vf::preload_plus_kernels();
+  if (e == cudaSuccess) e = vf::preload_batch_kernels();
+  if (e == cudaSuccess) e = vf::preload_probe_kernels();
+  if (e != cudaSuccess) return fail(VF_ERR_CUDA, "vf_preload: %s", cudaGetErrorString(e));
+  done[dev] = true;
+  return VF_OK;
+}
+
 int vf_device_info(int* sm, int* major, int* minor) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -228,12 +276,16 @@ int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, 
   return VF_OK;
 }
 
-int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n_events,
-              long long ev_offset, double xjac, const double* xmin, const double* xdelta,
-              double xdeltajac, const double* u_inj, unsigned long long seed,
-              unsigned int call_ctr, int integrand, const double* params, int train,
-              int accumulate, double* partials, int rows, int* ind_out, void* x_out,
-              void* w_out, void* f_out, int* flags, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// vf_sample, with the Philox call counter optionally in device memory.
+int sample_impl(int alg, int precision, const double* grid, int n_dim, long long n_events, long long ev_offset,
+                double xjac, const double* xmin, const double* xdelta, double xdeltajac, const double* u_inj,
+                unsigned long long seed, unsigned int call_ctr, const unsigned int* call_dev, int integrand,
+                const double* params, int train, int accumulate, double* partials, int rows, int* ind_out,
+                void* x_out, void* w_out, void* f_out, int* flags, void* stream) {
   if (alg != VF_ALG_VEGAS && alg != VF_ALG_PLAIN) return fail(VF_ERR_ARG, "vf_sample: alg=%d", alg);
   if (precision != VF_PREC_F64 && precision != VF_PREC_F32)
     return fail(VF_ERR_ARG, "vf_sample: precision=%d", precision);
@@ -283,6 +335,7 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   a.accumulate = accumulate ? 1 : 0;
   a.tma_swizzle = 0;
   a.rows_total = rows;
+  a.call_dev = call_dev;
   fill_philox(a, seed, call_ctr);
   if (jit) {
     if (taps && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS)
@@ -329,6 +382,21 @@ int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n
   return check_launch("vf_sample");
 }
 
+}  // namespace
+
+extern "C" {
+
+int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n_events,
+              long long ev_offset, double xjac, const double* xmin, const double* xdelta,
+              double xdeltajac, const double* u_inj, unsigned long long seed,
+              unsigned int call_ctr, int integrand, const double* params, int train,
+              int accumulate, double* partials, int rows, int* ind_out, void* x_out,
+              void* w_out, void* f_out, int* flags, void* stream) {
+  return sample_impl(alg, precision, grid, n_dim, n_events, ev_offset, xjac, xmin, xdelta, xdeltajac, u_inj, seed,
+                     call_ctr, nullptr, integrand, params, train, accumulate, partials, rows, ind_out, x_out, w_out,
+                     f_out, flags, stream);
+}
+
 int vf_reduce_events(int precision, const void* f, const void* w, const int* ind,
                      long long n_events, int n_dim, int n_out, int main_dim, int train,
                      int accumulate, double* partials, int rows, int* flags, void* stream) {
@@ -360,14 +428,20 @@ int vf_reduce_events(int precision, const void* f, const void* w, const int* ind
   return check_launch("vf_reduce_events");
 }
 
-int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int train,
-                     double n_events, double alpha, double* grid, double* hist_out,
-                     double* sums_out, double* history, double* avg, int iter, int* flags,
-                     void* stream) {
+}  // extern "C"
+
+namespace {
+
+// vf_iteration_end, with the iteration index (and the call counter it advances)
+// optionally in device memory.
+int iteration_end_impl(const double* partials, int rows, int n_dim, int n_out, int train, double n_events,
+                       double alpha, double* grid, double* hist_out, double* sums_out, double* history, double* avg,
+                       int iter, int* iter_dev, unsigned int* call_dev, int hist_cap, int* flags, void* stream) {
   if (!partials || rows < 1 || !history || !avg || iter < 0)
     return fail(VF_ERR_ARG, "vf_iteration_end: NULL buffer or bad rows/iter");
   if (n_dim < 1 || n_dim > VF_MAX_DIM) return fail(VF_ERR_UNSUPPORTED, "vf_iteration_end: n_dim=%d", n_dim);
   if (n_out < 1) return fail(VF_ERR_ARG, "vf_iteration_end: n_out=%d", n_out);
+  if (train < 0 || train > 2) return fail(VF_ERR_ARG, "vf_iteration_end: train=%d (0, 1 or 2)", train);
   if (train && !grid) return fail(VF_ERR_ARG, "vf_iteration_end: grid required when train");
   vf::IterEndArgs a;
   a.partials = partials;
@@ -382,11 +456,52 @@ int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int
   a.rows = rows;
   a.n_dim = n_dim;
   a.n_out = n_out;
-  a.train = train ? 1 : 0;
+  a.train = train == 2 ? 2 : (train ? 1 : 0);
   a.iter = iter;
+  a.iter_dev = iter_dev;
+  a.call_dev = call_dev;
+  a.hist_cap = hist_cap;
   const int clusters = (a.train || hist_out) ? n_dim + 1 : 1;
+  {
+    // the samplers run with the largest shared-memory carveout; the same
+    // preference here spares an L1/shared reconfiguration between the launches
+    static std::once_flag once;
+    std::call_once(once, [] {
+      cudaFuncSetAttribute(vf::vf_iteration_end_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared);
+    });
+  }
   vf::vf_iteration_end_kernel<<<clusters * VF_END_CLUSTER, VF_END_THREADS, 0, (cudaStream_t)stream>>>(a);
   return check_launch("vf_iteration_end");
+}
+
+}  // namespace
+
+extern "C" {
+
+int vf_iteration_end(const double* partials, int rows, int n_dim, int n_out, int train,
+                     double n_events, double alpha, double* grid, double* hist_out,
+                     double* sums_out, double* history, double* avg, int iter, int* flags,
+                     void* stream) {
+  return iteration_end_impl(partials, rows, n_dim, n_out, train, n_events, alpha, grid, hist_out, sums_out, history,
+                            avg, iter, nullptr, nullptr, 0, flags, stream);
+}
+
+int vf_iteration_dev(int alg, int precision, double* grid, int n_dim, long long n_events, double xjac,
+                     const double* xmin, const double* xdelta, double xdeltajac, unsigned long long seed,
+                     unsigned int* call_dev, int* iter_dev, int integrand, const double* params, int train,
+                     double alpha, double* partials, int rows, double* history, int hist_cap, double* avg,
+                     int* flags, void* stream) {
+  if (!call_dev || !iter_dev) return fail(VF_ERR_ARG, "vf_iteration_dev: call_dev and iter_dev are required");
+  if (hist_cap < 1) return fail(VF_ERR_ARG, "vf_iteration_dev: hist_cap=%d", hist_cap);
+  if (integrand == VF_INT_NONE) return fail(VF_ERR_ARG, "vf_iteration_dev: needs an integrand");
+  const int tr = alg == VF_ALG_VEGAS && train ? (precision == VF_PREC_F32 ? 2 : 1) : 0;
+  int rc = sample_impl(alg, precision, grid, n_dim, n_events, 0, xjac, xmin, xdelta, xdeltajac, nullptr, seed, 0,
+                       call_dev, integrand, params, tr != 0, 0, partials, rows, nullptr, nullptr, nullptr, nullptr, flags,
+                       stream);
+  if (rc) return rc;
+  return iteration_end_impl(partials, rows, n_dim, 1, tr, (double)n_events, alpha, grid, nullptr, nullptr, history,
+                            avg, 0, iter_dev, call_dev, hist_cap, flags, stream);
 }
 
 int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, int* flags,

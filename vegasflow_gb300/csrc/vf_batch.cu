@@ -125,3 +125,12 @@ int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, cons
 }
 
 }  // extern "C"
+
+namespace vf {
+cudaError_t preload_batch_kernels() {
+  cudaFuncAttributes attr;
+  cudaError_t e = cudaFuncGetAttributes(&attr, vf_batch_sample_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_batch_end_kernel);
+  return e;
+}
+}  // namespace vf

@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a)
     const double* partials = a.partials + 2 + role * VF_BINS;
     const long long* rows = a.tile_row + it.tile0;
     sum_hist_columns<5>([=](int k) { return partials + rows[k]; }, it.n_tiles, hsm, nullptr);
-    refine_dimension(hsm, a.grids + it.grid_off + role * VF_EDGES, a.alpha, a.flags);
+    refine_dimension_f32(hsm, a.grids + it.grid_off + role * VF_EDGES, a.alpha, a.flags);
     return;
   }
   double s1 = 0.0, s2 = 0.0;
@@ -291,10 +291,13 @@ __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a)
     }
     __syncthreads();
   }
+  __shared__ double s_mean;
+  __shared__ int s_hs;
+  const int slot = it.slot;
   if (t == 0) {
-    const int slot = it.slot;
     const int iter = a.iters[slot];
     const int hs = iter < a.hist_cap ? iter : a.hist_cap - 1;
+    s_hs = hs;
     const double res = red[0][0], res2 = red[1][0];
     const double N = (double)it.n_events;
     const double err = __ddiv_rn(__dsub_rn(__dmul_rn(N, res2), __dmul_rn(res, res)), __dsub_rn(N, 1.0));
@@ -309,16 +312,14 @@ __global__ void __launch_bounds__(256) vf_batch_end_kernel(const BatchEndArgs a)
     const double mean = av[0] / av[1];
     av[2] = mean;
     av[3] = sqrt(1.0 / av[1]);
-    double chi2 = 0.0;
-    for (int i = 0; i <= hs; ++i) {
-      const double* hi = a.history + ((long long)slot * a.hist_cap + i) * 2;
-      chi2 += (hi[0] - mean) * (hi[0] - mean) / (hi[1] * hi[1]);
-    }
-    av[4] = hs > 0 ? chi2 / hs : 0.0;
+    s_mean = mean;
     if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
     a.iters[slot] = iter + 1;
     a.calls[slot] += 1u;
   }
+  __syncthreads();
+  const double chi2 = block_chi2(a.history + (long long)slot * a.hist_cap * 2, 2, 1, s_hs + 1, s_mean);
+  if (t == 0) a.avg[5LL * slot + 4] = s_hs > 0 ? chi2 / s_hs : 0.0;
 }
 
 }  // namespace vf

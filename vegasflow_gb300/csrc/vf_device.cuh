@@ -23,6 +23,7 @@
 #define VF_FLAG_REFINE_OVERRUN 2  // the rebinning walk ran past the last bin
 #define VF_FLAG_NONFINITE 4    // a partial sum was NaN or Inf
 #define VF_FLAG_TIMEOUT 8      // a bounded wait gave up (a copy never completed)
+#define VF_FLAG_HISTORY_FULL 16  // an iteration found no history row left (nothing recorded)
 
 namespace vf {
 

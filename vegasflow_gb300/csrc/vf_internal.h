@@ -9,8 +9,6 @@ namespace vf {
 // (dmax in {4, 8, 16}; integrand a VF_INT_* id), or nullptr.
 const void* sample_kernel_f64(int dmax, int integrand);
 const void* sample_kernel_f32(int dmax, int integrand);
-const void* plus_kernel_f64(int dmax, int integrand);
-const void* plus_kernel_f32(int dmax, int integrand);
 
 // The fp32 VEGAS sampler specialised on the exact dimension count (1..8 in
 // part a, 9..16 in part b) and the block size (128 or 256 threads).
@@ -29,6 +27,12 @@ inline const void* vegas_f32_kernel(int n_dim, int integrand, int threads = 256)
 // histogram layout it uses.
 int jit_launch(int integrand_id, int alg, int precision, int n_dim, void* args, int rows, int train,
                void* stream, int* fast_out, int* hist_copies_inout);
+
+// Load (cudaFuncGetAttributes) every kernel of a translation unit on the
+// current device; return the first CUDA error, or cudaSuccess.
+cudaError_t preload_plus_kernels();
+cudaError_t preload_batch_kernels();
+cudaError_t preload_probe_kernels();
 
 // Records an error message for vf_last_error_string(); returns `code`.
 int set_error(int code, const char* message);

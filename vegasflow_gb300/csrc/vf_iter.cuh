@@ -23,8 +23,14 @@ struct IterEndArgs {
   int rows;
   int n_dim;
   int n_out;
-  int train;
+  int train;               // 0 no refinement, 1 refine in float64, 2 refine in float32
   int iter;
+  // nullable: the iteration index in device memory (read instead of `iter`,
+  // then advanced, with the Philox call counter `call_dev`, for the next
+  // iteration: a launch replayed from a CUDA graph); history has hist_cap rows
+  int* iter_dev;
+  unsigned int* call_dev;
+  int hist_cap;
 };
 
 // The iteration-end kernel runs in clusters of VF_END_CLUSTER blocks: cluster
@@ -65,12 +71,19 @@ vf_iteration_end_kernel(const IterEndArgs a) {
       if (a.hist_out) a.hist_out[d * VF_BINS + t] = v;
     }
     cluster.sync();  // the other blocks keep their shared memory until block 0 has read it
-    if (rank == 0 && a.train) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
+    if (rank == 0 && a.train == 1) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
+    if (rank == 0 && a.train == 2) refine_dimension_f32(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
     return;
   }
   if (rank != 0) return;
+  const int it = a.iter_dev ? *a.iter_dev : a.iter;
+  if (it < 0 || (a.iter_dev && it >= a.hist_cap)) {  // no history row left: report, change nothing
+    if (t == 0 && a.flags) atomicOr(a.flags, VF_FLAG_HISTORY_FULL);
+    return;
+  }
   // ---- the sums, one output at a time
   __shared__ double red[2][VF_END_THREADS / 32];
+  __shared__ double mean_sh;
   const int lane = t & 31, warp = t >> 5;
   for (int j = 0; j < K; ++j) {
     double s1 = 0.0, s2 = 0.0;
@@ -102,7 +115,7 @@ vf_iteration_end_kernel(const IterEndArgs a) {
         a.sums_out[j] = res;
         a.sums_out[K + j] = res2;
       }
-      double* hrow = a.history + (long long)a.iter * 2 * K;
+      double* hrow = a.history + (long long)it * 2 * K;
       hrow[j] = res;
       hrow[K + j] = sigma;
       // monte_carlo.py:712-732, accumulated iteration by iteration
@@ -113,18 +126,18 @@ vf_iteration_end_kernel(const IterEndArgs a) {
       const double mean = av[0] / av[1];
       av[2] = mean;
       av[3] = sqrt(1.0 / av[1]);
-      double chi2 = 0.0;
-      for (int i = 0; i <= a.iter; ++i) {
-        const double r = a.history[(long long)i * 2 * K + j];
-        const double sg = a.history[(long long)i * 2 * K + K + j];
-        chi2 += (r - mean) * (r - mean) / (sg * sg);
-      }
-      av[4] = a.iter > 0 ? chi2 / a.iter : 0.0;
+      mean_sh = mean;
       if (!isfinite(res) || !isfinite(res2)) {
         if (a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
       }
     }
     __syncthreads();
+    const double chi2 = block_chi2(a.history + j, 2 * K, K, it + 1, mean_sh);
+    if (t == 0) a.avg[5 * j + 4] = it > 0 ? chi2 / it : 0.0;
+  }
+  if (t == 0 && a.iter_dev) {  // the next iteration's index and Philox call
+    *a.iter_dev = it + 1;
+    if (a.call_dev) *a.call_dev += 1u;
   }
 }
 

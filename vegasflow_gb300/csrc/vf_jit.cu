@@ -148,9 +148,13 @@ int jit_launch(int integrand_id, int alg, int precision, int n_dim, void* args, 
   }
   const Driver& drv = driver();
   if (!drv.ok) return set_error(VF_ERR_CUDA, "CUDA driver entry points unavailable");
-  if (smem > 48 * 1024 &&
-      drv.func_set_attribute(k.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS)
-    return set_error(VF_ERR_CUDA, "cuFuncSetAttribute for a JIT kernel failed");
+  if (smem > 48 * 1024 && k.smem_set < smem) {  // once per size: no attribute call in later (captured) launches
+    if (drv.func_set_attribute(k.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS)
+      return set_error(VF_ERR_CUDA, "cuFuncSetAttribute for a JIT kernel failed");
+    std::lock_guard<std::mutex> lock(g_mu);
+    JitKernel& kk = g_kernels[integrand_id - VF_INT_JIT_BASE];
+    if (kk.smem_set < smem) kk.smem_set = smem;
+  }
   void* params[] = {args};
   const CUresult r =
       drv.launch_kernel(k.fn, rows, 1, 1, VF_THREADS, 1, 1, smem, (CUstream)stream, params, nullptr);

@@ -194,3 +194,22 @@ int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, lo
 }
 
 }  // extern "C"
+
+namespace vf {
+cudaError_t preload_plus_kernels() {
+  cudaFuncAttributes attr;
+  for (int prec = 0; prec < 2; ++prec)
+    for (int dmax : {4, 8, 16})
+      for (int integ = VF_INT_NONE; integ <= VF_INT_SUM; ++integ) {
+        const void* k = ::plus_kernel(prec ? VF_PREC_F32 : VF_PREC_F64, dmax, integ);
+        if (k) {
+          const cudaError_t e = cudaFuncGetAttributes(&attr, k);
+          if (e != cudaSuccess) return e;
+        }
+      }
+  cudaError_t e = cudaFuncGetAttributes(&attr, vf_plus_reduce_kernel<double>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_plus_reduce_kernel<float>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_plus_iteration_end_kernel);
+  return e;
+}
+}  // namespace vf

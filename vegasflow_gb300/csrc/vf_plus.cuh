@@ -301,6 +301,7 @@ __global__ void __launch_bounds__(256) vf_plus_iteration_end_kernel(const PlusEn
   }
   __shared__ double red[3][256];
   __shared__ double s_sum_damped;
+  __shared__ double s_mean;
   __shared__ long long scan[256];
   // res = sum ress, sigma^2 = sum max(var, 0) / (n_ev - 1)   (vflowplus.py:230-233)
   double r1 = 0.0, r2 = 0.0, r3 = 0.0;
@@ -336,16 +337,15 @@ __global__ void __launch_bounds__(256) vf_plus_iteration_end_kernel(const PlusEn
     const double mean = a.avg[0] / a.avg[1];
     a.avg[2] = mean;
     a.avg[3] = sqrt(1.0 / a.avg[1]);
-    double chi2 = 0.0;
-    for (int i = 0; i <= a.iter; ++i) {
-      const double r = a.history[2 * i], sg = a.history[2 * i + 1];
-      chi2 += (r - mean) * (r - mean) / (sg * sg);
-    }
-    a.avg[4] = a.iter > 0 ? chi2 / a.iter : 0.0;
+    s_mean = mean;
     if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
     s_sum_damped = red[2][0];
   }
   __syncthreads();
+  {
+    const double chi2 = block_chi2(a.history, 2, 1, a.iter + 1, s_mean);
+    if (t == 0) a.avg[4] = a.iter > 0 ? chi2 / a.iter : 0.0;
+  }
   if (!a.adaptive) return;
   // vflowplus.py:157-163: n_ev = int(max(min_neval, d^(beta/2) N0 / 2 / sum d))
   const double sum_d = s_sum_damped;

@@ -3,6 +3,7 @@
 // one warp instruction per clock.  Used by bench.py to measure the achievable
 // warp-instruction rate at the clocks of the run.
 #include "vegasflow_gb300.h"
+#include "vf_internal.h"
 
 #include <cuda_runtime.h>
 
@@ -33,3 +34,10 @@ extern "C" int vf_issue_probe(float* out, int blocks, int iters, long long* fma_
   if (fma_per_thread) *fma_per_thread = 8LL * 16LL * iters;
   return cudaGetLastError() == cudaSuccess ? VF_OK : VF_ERR_LAUNCH;
 }
+
+namespace vf {
+cudaError_t preload_probe_kernels() {
+  cudaFuncAttributes attr;
+  return cudaFuncGetAttributes(&attr, vf_issue_probe_kernel);
+}
+}  // namespace vf

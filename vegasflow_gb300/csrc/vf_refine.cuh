@@ -38,6 +38,31 @@ __device__ inline void sum_hist_columns(RowAt row_at, int rows, double* hsm, dou
   __syncthreads();
 }
 
+// chi^2 of `count` history rows against `mean`: sum over rows i of
+// (r_i - mean)^2 / sigma_i^2, r_i = rows[i stride], sigma_i = rows[i stride +
+// sig_off].  Rows are spread over the block's threads, then added lane by lane
+// and warp by warp (a fixed order); every thread of the block calls it, the
+// total is valid in thread 0.  (Each row costs a float64 division, ~1,000
+// cycles on this part: one thread walking a long history was the iteration
+// end's slowest step.)
+__device__ inline double block_chi2(const double* rows, long long stride, int sig_off, int count, double mean) {
+  __shared__ double part[32];
+  double c = 0.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) {
+    const double r = rows[(long long)i * stride], sg = rows[(long long)i * stride + sig_off];
+    c += (r - mean) * (r - mean) / (sg * sg);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+  __syncthreads();
+  double total = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += part[w];
+  __syncthreads();
+  return total;
+}
+
 // Sum of 50 values in NumPy's order for a contiguous float64 array of that
 // length (np.sum: eight strided accumulators, a fixed tree, then the two
 // remaining values), so the result is the oracle's bit for bit.  Called by
@@ -135,6 +160,115 @@ __device__ inline void refine_dimension(const double* h, double* row, double alp
   } else if (t == VF_BINS - 1) {
     row[0] = 0.0;
   } else if (t == VF_BINS) {
+    row[VF_BINS] = 1.0;
+  }
+  __syncthreads();
+}
+
+// The same refinement in float32 arithmetic -- the reference's float32 mode
+// (configflow.py float switch) -- for the fp32 sampler's grids: the float64
+// histogram is scaled by a power of two so its largest bin is about 1 (the
+// refinement depends only on ratios, apart from the 1e-30 floor, which then
+// applies relative to the largest bin), the smoothing, logarithms, damping and
+// the rebinning walk run in float32 (a few hundred cycles instead of the
+// float64 pipe's ~15,000 on this part), and the new edges are made
+// non-decreasing before they are stored as float64.
+__device__ inline float sum50_pairwise_f(const float* v) {
+  const int j = threadIdx.x & 31;
+  float r = 0.0f;
+  if (j < 8) {
+    r = v[j];
+    for (int i = 8; i < 48; i += 8) r += v[i + j];
+  }
+  r += __shfl_down_sync(0xffffffffu, r, 1);
+  r += __shfl_down_sync(0xffffffffu, r, 2);
+  r += __shfl_down_sync(0xffffffffu, r, 4);
+  r += v[48];
+  r += v[49];
+  return r;
+}
+
+__device__ inline void refine_dimension_f32(const double* h, double* row, double alpha, int* flags) {
+  __shared__ float sub[VF_EDGES];
+  __shared__ float hf[VF_BINS];
+  __shared__ float sm[VF_BINS];
+  __shared__ float wei[VF_BINS];
+  __shared__ float edge[VF_EDGES];
+  __shared__ float sum_t;
+  __shared__ int emax;
+  __shared__ int walk_bin[VF_BINS - 1];
+  __shared__ float walk_weight[VF_BINS - 1];
+  const int t = threadIdx.x;
+  if (t < VF_EDGES) sub[t] = (float)row[t];
+  if (t < 32) {  // the largest binary exponent among the 50 bins (integer max over the bit patterns)
+    int e = -1022;
+    for (int b = t; b < VF_BINS; b += 32) {
+      const int ex = (int)((__double_as_longlong(h[b]) >> 52) & 0x7FF) - 1023;
+      e = ex > e ? ex : e;
+    }
+    e = __reduce_max_sync(0xffffffffu, e);
+    if (t == 0) emax = e > 1000 ? 1000 : e;
+  }
+  __syncthreads();
+  if (t < VF_BINS) hf[t] = (float)(h[t] * __longlong_as_double((long long)(1023 - emax) << 52));  // h 2^-emax
+  __syncthreads();
+  if (t < VF_BINS) {
+    const float left = t > 0 ? hf[t - 1] : 0.0f;
+    const float right = t < VF_BINS - 1 ? hf[t + 1] : 0.0f;
+    const float v = (hf[t] + right) + left;
+    const float meaner = (t == 0 || t == VF_BINS - 1) ? 2.0f : 3.0f;
+    sm[t] = fmaxf(v / meaner, 1e-30f);
+  }
+  __syncthreads();
+  if (t < 32) {
+    const float s = sum50_pairwise_f(sm);
+    if (t == 0) sum_t = s;
+  }
+  __syncthreads();
+  if (t < VF_BINS) {
+    const float aux = (1.0f - sm[t] / sum_t) / (logf(sum_t) - logf(sm[t]));
+    wei[t] = alpha == 1.5 ? aux * sqrtf(aux) : powf(aux, (float)alpha);
+  }
+  __syncthreads();
+  if (t < 32) {
+    const float total = sum50_pairwise_f(wei);
+    if (t == 0) {
+      const float ave = total / VF_BINS;
+      float bin_weight = 0.0f;
+      int n_bin = -1;
+      int overrun = 0;
+      for (int k = 0; k < VF_BINS - 1; ++k) {
+        while (bin_weight < ave) {
+          if (n_bin + 1 >= VF_BINS) {
+            overrun = 1;
+            break;
+          }
+          n_bin += 1;
+          bin_weight += wei[n_bin];
+        }
+        bin_weight -= ave;
+        walk_bin[k] = n_bin;
+        walk_weight[k] = bin_weight;
+      }
+      if (overrun && flags) atomicOr(flags, VF_FLAG_REFINE_OVERRUN);
+    }
+  }
+  __syncthreads();
+  if (t < VF_BINS - 1) {
+    const int n_bin = walk_bin[t];
+    const float cur = n_bin >= 0 ? sub[n_bin + 1] : 0.0f;
+    const float prev = n_bin >= 1 ? sub[n_bin] : 0.0f;
+    const float w = wei[n_bin >= 0 ? n_bin : VF_BINS - 1];
+    edge[t + 1] = cur - (cur - prev) * walk_weight[t] / w;
+  }
+  __syncthreads();
+  if (t == 0) {  // float32 rounding can swap two edges a few ulps apart: keep them ordered
+    float lo = 0.0f;
+    row[0] = 0.0;
+    for (int k = 1; k < VF_BINS; ++k) {
+      lo = fmaxf(lo, fminf(edge[k], 1.0f));
+      row[k] = (double)lo;
+    }
     row[VF_BINS] = 1.0;
   }
   __syncthreads();

@@ -50,6 +50,10 @@ struct SampleArgs {
   unsigned int ctr2[8];     // Philox counter word 2 of 4-word block q: (call << 4) | q;
                             // float64 uses ceil(D/2) <= 8 blocks, fp32 ceil(D/4) <= 4
   unsigned int ctr3;        // Philox counter word 3: call >> 28
+  // nullable: the call counter in device memory, read by the kernel instead of
+  // ctr2/ctr3 (a launch replayed from a CUDA graph, where the counter advances
+  // on the device)
+  const unsigned int* call_dev;
   // fp32 VEGAS kernel with injected uniforms: 0 = plain loads; 1|2|3 = tiles of
   // THREADS events brought into shared memory by TMA through `tmap`, with the
   // 32|64|128-byte swizzle (row bytes 8 D = 32|64|128)
@@ -59,9 +63,21 @@ struct SampleArgs {
   alignas(64) unsigned long long tmap[16];
 };
 
-// The 4 words of block q of event ev, with the host-computed keys/counters.
-__device__ __forceinline__ void philox_words(u64 ev, const SampleArgs& a, int q, u32 w[4]) {
-  u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+// Philox counter words 2 (block 0; block q adds q) and 3 of a launch.
+struct CallWords {
+  u32 c2base, c3;
+};
+__device__ __forceinline__ CallWords call_words(const SampleArgs& a) {
+  if (a.call_dev) {
+    const u32 call = *a.call_dev;
+    return {call << 4, call >> 28};
+  }
+  return {a.ctr2[0], a.ctr3};
+}
+
+// The 4 words of block q of event ev, with the host-computed keys.
+__device__ __forceinline__ void philox_words(u64 ev, const SampleArgs& a, const CallWords& cw, int q, u32 w[4]) {
+  u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = cw.c2base | (u32)q, c3 = cw.c3;
   philox4x32_10_rk(c0, c1, c2, c3, a.rk);
   w[0] = c0;
   w[1] = c1;
@@ -134,6 +150,7 @@ vf_sample_kernel(const SampleArgs a) {
   const bool fill_hist = evaluate && vegas && a.train;
   const bool limits = (a.xmin != nullptr);
   const int nb = D * VF_BINS;
+  const CallWords cw = call_words(a);
 
   // shared-memory carve-up
   unsigned char* p = smem;
@@ -199,7 +216,7 @@ vf_sample_kernel(const SampleArgs a) {
         for (int q = 0; q < (DMAX + 1) / 2; ++q)
           if (2 * q < D) {
             u32 wd[4];
-            philox_words(ev, a, q, wd);
+            philox_words(ev, a, cw, q, wd);
             u[2 * q] = tech_cut(u53(wd[0], wd[1]));
             if (2 * q + 1 < DMAX) u[2 * q + 1] = tech_cut(u53(wd[2], wd[3]));
           }
@@ -284,7 +301,7 @@ vf_sample_kernel(const SampleArgs a) {
         for (int q = 0; q < (DMAX + 3) / 4; ++q)
           if (4 * q < D) {
             u32 r[4];
-            philox_words(ev, a, q, r);
+            philox_words(ev, a, cw, q, r);
 #pragma unroll
             for (int j = 0; j < 4; ++j)
               if (4 * q + j < DMAX) wd[4 * q + j] = r[j];

@@ -148,6 +148,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
   const bool train = a.train != 0;
   const bool limits = a.xmin != nullptr;
   const int cpw = a.hist_copies;
+  const CallWords cw = call_words(a);
   const bool fixedp = train && cpw == VF_F32_HIST_FIXED;
   // fixed-point layout: integer joint tables (as layout 0), float overflow table [NB]
   u32* hint = reinterpret_cast<u32*>(hist);
@@ -268,7 +269,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
   auto draw = [&](u64 ev, int (&bins)[D], float& wf, float& s, float (&x)[D]) {
 #pragma unroll
     for (int q = 0; q < (D + 3) / 4; ++q) {
-      u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+      u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = cw.c2base | (u32)q, c3 = cw.c3;
       philox4x32_10_rk(c0, c1, c2, c3, a.rk);
       const u32 wq[4] = {c0, c1, c2, c3};
 #pragma unroll

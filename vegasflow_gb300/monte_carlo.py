@@ -59,6 +59,10 @@ def print_iteration(it, res, error, extra="", threshold=0.1):
     return f"Result for iteration {it}: {res:.4f} +/- {error:.4f}" + extra
 
 
+# the fewest events per launched block of a sampler (256 threads x 4)
+EVENTS_PER_BLOCK_MIN = 1024
+
+
 def _chunk_sizes(n_events, events_per_run):
     """monte_carlo.py:437-452."""
     out = []
@@ -79,10 +83,11 @@ class MonteCarloFlow(ABC):
     _CAN_RUN_VECTORIAL = False
     _ALG = nat.VF_ALG_PLAIN
     _FUSED_F32_SAMPLER = False  # launches the fused fp32 VEGAS sampler (has a launch shape)
+    _GRAPH_ITERATIONS = False  # one iteration is vf_iteration_dev (CUDA-graph replayable)
 
     def __init__(self, n_dim, n_events, events_limit=MAX_EVENTS_LIMIT,
                  list_devices=DEFAULT_ACTIVE_DEVICES, verbose=True, xmin=None, xmax=None,
-                 precision=None, device=None, seed=None, autotune=False, **kwargs):
+                 precision=None, device=None, seed=None, autotune=False, cuda_graph=False, **kwargs):
         if "simplify_signature" in kwargs:
             logger.warning("simplify_signature is deprecated and will be removed")
         self.n_dim = int(n_dim)
@@ -121,6 +126,9 @@ class MonteCarloFlow(ABC):
         self._it = 0
         self._autotune = bool(autotune)
         self._shape = None
+        self._cuda_graph = bool(cuda_graph)
+        self._graph = None
+        self._graph_key = None
 
         if xmin is not None or xmax is not None:  # monte_carlo.py:159-175
             if xmin is None or xmax is None:
@@ -332,8 +340,10 @@ class MonteCarloFlow(ABC):
         """Iteration-end kernel; returns (res, sigma) device views of the history row."""
         ws = self._history_slot()
         n = float(self.n_events if n_events is None else n_events)
+        # the fp32 form refines its grid in float32 (the reference's float32 arithmetic)
+        mode = (2 if self._prec == nat.VF_PREC_F32 else 1) if train else 0
         nat.call("vf_iteration_end", nat.ptr(ws["partials"]), self._rows, self.n_dim, self._n_out,
-                 int(bool(train)), n, float(ALPHA), self._grid_ptr(),
+                 mode, n, float(ALPHA), self._grid_ptr(),
                  nat.ptr(ws["hist"]) if want_hist else None, nat.ptr(ws["sums"]) if want_sums else None,
                  nat.ptr(ws["history"]), nat.ptr(ws["avg"]), int(self._it), nat.ptr(ws["flags"]),
                  nat.stream_handle())
@@ -507,7 +517,10 @@ class MonteCarloFlow(ABC):
         rows = ctypes.c_int(0)
         integ = self._int_id if self._kind == "device" else nat.VF_INT_SYMGAUSS
         nat.check(lib.vf_sample_rows(self._ALG, self._prec, self.n_dim, integ, 1, ctypes.byref(rows)))
-        self._rows = max(1, rows.value)
+        # a small iteration launches no more blocks than give every thread a few
+        # events: idle blocks still stage the table, clear and read back their
+        # histogram, and add partial rows for the iteration end to reduce
+        self._rows = max(1, min(rows.value, -(-self.n_events // EVENTS_PER_BLOCK_MIN)))
 
     def _recompile(self):
         if self._compilation_arguments is None:
@@ -515,13 +528,84 @@ class MonteCarloFlow(ABC):
         self.compile(self._compilation_arguments[0], **self._compilation_arguments[1])
 
     # ---------------------------------------------------------------- integration
+    # ---------------------------------------------------------------- CUDA-graph iterations
+    def _graph_ready(self, histograms):
+        return (self._cuda_graph and self._GRAPH_ITERATIONS and self._kind == "device" and not histograms
+                and self._uniform_source is None and self.device.type == "cuda")
+
+    def _graph_call(self, ws):
+        xmin, xdelta, xdj = self._limits_ptrs()
+        nat.call("vf_iteration_dev", self._ALG, self._prec, self._grid_ptr(), self.n_dim, int(self.n_events),
+                 float(self.xjac), xmin, xdelta, float(xdj), self._seed, nat.ptr(ws["counters"][0:1]),
+                 nat.ptr(ws["counters"][1:2]), int(self._int_id), nat.ptr(self._params_dev),
+                 int(bool(self._train_now())), float(ALPHA), nat.ptr(ws["partials"]), self._rows,
+                 nat.ptr(ws["history"]), int(ws["history"].shape[0]), nat.ptr(ws["avg"]), nat.ptr(ws["flags"]),
+                 nat.stream_handle())
+
+    def _graph_for(self, n_iter):
+        """The CUDA graph of one iteration (captured again whenever an argument
+        of the captured call changed), with room for ``n_iter`` history rows."""
+        ws = self._workspace()
+        if ws["history"].shape[0] < n_iter:
+            ws["history"] = torch.zeros((max(n_iter, 2 * ws["history"].shape[0]), 2 * self._n_out),
+                                        dtype=torch.float64, device=self.device)
+        if "counters" not in ws:
+            ws["counters"] = torch.zeros(2, dtype=torch.int32, device=self.device)
+        self._apply_shape()
+        def addr(p):
+            return p.value if p is not None else 0
+
+        xmin, xdelta, xdj = self._limits_ptrs()
+        key = (self._ALG, self._prec, addr(self._grid_ptr()), self.n_events, self.xjac, self._seed, self._int_id,
+               self._params_dev.data_ptr(), bool(self._train_now()), self._rows, ws["partials"].data_ptr(),
+               ws["history"].data_ptr(), ws["history"].shape[0], ws["avg"].data_ptr(), ws["flags"].data_ptr(),
+               ws["counters"].data_ptr(), addr(xmin), addr(xdelta), xdj, self._shape)
+        if self._graph is None or self._graph_key != key:
+            from .utils import preload_kernels
+            preload_kernels(self.device)
+            torch.cuda.synchronize(self.device)
+            side = torch.cuda.Stream(device=self.device)
+            side.wait_stream(torch.cuda.current_stream(self.device))
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(side):
+                with torch.cuda.graph(g, stream=side):
+                    self._graph_call(ws)
+            torch.cuda.current_stream(self.device).wait_stream(side)
+            self._graph, self._graph_key = g, key
+        return self._graph, ws
+
+    def _run_graph(self, n_iter, log_time):
+        """``n_iter`` iterations as replays of one captured iteration: the Philox
+        call counter and the history row advance on the device."""
+        g, ws = self._graph_for(n_iter)
+        start = np.array([self._call_ctr & 0xFFFFFFFF, self._it], dtype=np.uint32).view(np.int32)
+        ws["counters"].copy_(torch.from_numpy(start))
+        for i in range(n_iter):
+            if log_time:
+                t0 = time.time()
+            g.replay()
+            self._history.append([None, None, None])
+            if self._verbose:
+                row = ws["history"][self._it + i].cpu().numpy()
+                time_str = f"(took {time.time() - t0:.5f} s)" if log_time else ""
+                logger.info(print_iteration(i, float(row[0]), float(row[1]), extra=time_str))
+        self._call_ctr += n_iter
+        self._it += n_iter
+
     def run_integration(self, n_iter, log_time=True, histograms=None):
-        """Run ``n_iter`` iterations; returns (result, sigma) (monte_carlo.py:645-741)."""
+        """Run ``n_iter`` iterations; returns (result, sigma) (monte_carlo.py:645-741).
+
+        With ``cuda_graph=True`` (device integrands, VegasFlow and PlainFlow) the
+        iterations are replays of one captured CUDA graph (two kernels, no host
+        work between iterations)."""
         self._require_gpu()
         self._reset_average()
         first = len(self._history)
         all_results = []
-        for i in range(n_iter):
+        graph = self._graph_ready(histograms)
+        if graph:
+            self._run_graph(n_iter, log_time)
+        for i in range(0 if graph else n_iter):
             if log_time:
                 start = time.time()
             res, error = self._run_iteration()

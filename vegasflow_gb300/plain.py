@@ -11,6 +11,7 @@ class PlainFlow(MonteCarloFlow):
 
     _CAN_RUN_VECTORIAL = True
     _ALG = nat.VF_ALG_PLAIN
+    _GRAPH_ITERATIONS = True
 
     def _run_event(self, integrand, ncalls=None):
         return self.run_event()

@@ -27,6 +27,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from .utils import preload_kernels
 from .batch import DEFAULT_TILE_EVENTS, ITEM_DTYPE
 from .configflow import BINS_MAX
 from .integrands import DeviceIntegrand
@@ -128,6 +129,7 @@ class VegasServer:
         if self.device.type != "cuda":
             raise RuntimeError("VegasServer runs on a CUDA device only")
         nat.load()
+        preload_kernels(self.device)
         self.max_slots = int(max_slots)
         self.hbm_budget = float(hbm_budget)
         self.tile_events = int(tile_events)

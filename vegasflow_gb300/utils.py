@@ -28,3 +28,43 @@ def consume_array_into_indices(input_arr, indices, result_size):
 def py_consume_array_into_indices(input_arr, indices, result_size):
     """Python-object interface of ``consume_array_into_indices`` (utils.py:47-52)."""
     return consume_array_into_indices(input_arr, indices, int(result_size))
+
+
+_PRELOADED = set()
+
+
+def preload_kernels(device):
+    """Load, once per device and before the first CUDA-graph capture, every
+    kernel of the native library (``vf_preload``) and run the small torch
+    operations the integrators, the batch engine and the server use
+    around their own kernels (advanced-index writes and gathers, casts,
+    concatenation, fills, strided copies) for the dtypes they use.
+
+    With lazy module loading (the default), the first use of a kernel loads its
+    module; measured on GB300 with driver 580, a module loaded after a CUDA graph
+    has been captured in the process took ~2.2 s (50 ms before), which showed up
+    as a 2-second stall in the first admission of a server started after a
+    graph-replayed batch.  Loading these modules up front keeps that out of the
+    timed paths."""
+    dev = torch.device(device)
+    if dev.type != "cuda":
+        return
+    key = (dev.index if dev.index is not None else torch.cuda.current_device())
+    if key in _PRELOADED:
+        return
+    with torch.cuda.device(dev):
+        nat.check(nat.load().vf_preload())  # the library's own kernels
+    idx = torch.zeros(1, dtype=torch.int64, device=dev)
+    for dt in (torch.float64, torch.float32, torch.int32, torch.int64, torch.uint8):
+        a = torch.zeros((4, 3, 2), dtype=dt, device=dev)
+        a[idx] = torch.ones((1, 3, 2), dtype=dt, device=dev)  # index_put, tensor source
+        a[idx] = 0  # index_put, scalar source
+        b = a[idx][:, 1:2].reshape(-1)  # gather, strided copy
+        c = torch.cat([b, a.reshape(-1)])  # concatenation
+        for dt2 in (torch.float64, torch.float32, torch.int32):
+            c.to(dt2)  # casts
+        a.fill_(1)
+        a.copy_(a.clone())
+        a.view(4, 6)[:, 2:4].contiguous()
+    torch.cuda.synchronize(dev)
+    _PRELOADED.add(key)

@@ -27,6 +27,7 @@ class VegasFlow(MonteCarloFlow):
 
     _ALG = nat.VF_ALG_VEGAS
     _FUSED_F32_SAMPLER = True
+    _GRAPH_ITERATIONS = True
 
     def __init__(self, n_dim, n_events, train=True, main_dimension=0, **kwargs):
         super().__init__(n_dim, n_events, **kwargs)

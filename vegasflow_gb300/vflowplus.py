@@ -47,6 +47,7 @@ class VegasFlowPlus(VegasFlow):
     """VEGAS+ (vflowplus.py:83)."""
 
     _FUSED_F32_SAMPLER = False  # samples per hypercube through its own kernels
+    _GRAPH_ITERATIONS = False
 
     def __init__(self, n_dim, n_events, train=True, adaptive=False, events_limit=None, **kwargs):
         if events_limit is None:  # vflowplus.py:89-99
