@@ -315,6 +315,8 @@ def main():
         # end-to-end through the public API with a host-resident grid
         e2e = e2e_run(inst32, K, dev)
         injected = None if args.no_injected else injected_run(dev, args.events, K, W)
+        sampler = None if args.no_injected else sampler_run(dev, args.events, K, W)
+        configs = None if args.no_batched else configs_run(dev)
     clk = clocks.summary()
 
     total32 = float(t32.sum())
@@ -351,6 +353,8 @@ def main():
                      "sampler_ms": 1e3 * samp_mean},
         "e2e": e2e,
         "injected": injected,
+        "sampler": sampler,
+        "configs": configs,
         "gpu_launches": 2 * K,
         "clocks": clk,
     }
@@ -449,6 +453,90 @@ def injected_run(dev, n_events, K, W, seed=11):
                                      "launch equals them to within 1% (profiles/vegas_fp32_injected.md)",
                      "peak_source": source},
     }
+
+
+def sampler_run(dev, n_events, K, W, seed=3):
+    """The sampler API (VEGAS as a random-number generator): on a trained
+    8-D grid, ``generate_random_array(n)`` writes x (8 floats) and the weight
+    (1 float) of every event to HBM -- one map kernel launch plus the weight
+    normalisation.  ``value`` is through the public call; the roofline is the
+    map kernel alone (36 bytes written per event)."""
+    import torch
+
+    from vegasflow_gb300 import VegasFlow, integrands
+    from vegasflow_gb300 import _native as nat
+
+    inst = VegasFlow(N_DIM, n_events, verbose=False, precision="fp32", seed=seed, device=dev)
+    inst.compile(integrands.symgauss(A_WIDTH))
+    for _ in range(2):
+        inst._run_iteration()
+    stream = torch.cuda.current_stream()
+    x = torch.empty((n_events, N_DIM), dtype=torch.float32, device=dev)
+    w = torch.empty(n_events, dtype=torch.float32, device=dev)
+    for k in range(W):
+        inst.generate_random_array(n_events)
+        inst._sample(n_events, 0, 900 + k, nat.VF_INT_NONE, None, False, False, x=x, w=w)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for k in range(K):
+        xr, pr = inst.generate_random_array(n_events)
+    b.record(stream)
+    b.synchronize()
+    api_ms = a.elapsed_time(b) / K
+    del xr, pr
+    a.record(stream)
+    for k in range(K):
+        inst._sample(n_events, 0, 950 + k, nat.VF_INT_NONE, None, False, False, x=x, w=w)
+    b.record(stream)
+    b.synchronize()
+    kern_ms = a.elapsed_time(b) / K
+    del x, w
+    torch.cuda.empty_cache()
+    bytes_per_event = 4 * N_DIM + 4
+    achieved = bytes_per_event * n_events / (kern_ms / 1e3) / 1e9
+    peak, source = measured_hbm_peak()
+    return {
+        "workload": f"generate_random_array({n_events:.0e}) on a trained {N_DIM}-D grid, fp32 x and weight",
+        "value": n_events / (api_ms / 1e3), "unit": "events/s", "ms_per_call": api_ms, "kernel_ms": kern_ms,
+        "roofline": {"bound": "hbm", "kernel": "vf_vegas_f32_map_kernel<8>", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": bytes_per_event * n_events,
+                     "traffic_note": "algorithmic bytes written (x 32 B + w 4 B per event)",
+                     "peak_source": source},
+    }
+
+
+def configs_run(dev):
+    """The other configurations of the metric, briefly: C1 (4-D Gaussian,
+    float64, 1e6 events x 5 iterations, seed 7) and C3 (VegasFlowPlus adaptive,
+    6-D Breit-Wigner x linear, 2e6 events x 10 iterations) in both precisions,
+    each against its exact value."""
+    import numpy as np
+    import torch
+
+    from vegasflow_gb300 import VegasFlow, VegasFlowPlus, integrands
+
+    out = {}
+    exact1 = math.erf(0.5 / A_WIDTH) ** 4
+    coeffs = np.random.default_rng(3).random(5)
+    exact3 = integrands.breit_wigner_exact(6, coeffs)
+    for name, make, it, exact in (
+            ("C1", lambda p: (VegasFlow(4, 1_000_000, verbose=False, precision=p, seed=7, device=dev),
+                              integrands.symgauss(A_WIDTH)), 5, exact1),
+            ("C3", lambda p: (VegasFlowPlus(6, 2_000_000, adaptive=True, verbose=False, precision=p, seed=7,
+                                            device=dev), integrands.breit_wigner(coeffs)), 10, exact3)):
+        for prec in ("fp64", "fp32"):
+            inst, f = make(prec)
+            inst.compile(f)
+            inst.run_integration(1)  # warm-up (compile-time work, first launches)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res, sig = inst.run_integration(it)
+            dt = time.perf_counter() - t0
+            events = sum(int(h) for h in [inst.n_events] * it)
+            out[f"{name}_{prec}"] = {"events_per_s": events / dt, "seconds": dt, "mean": float(res),
+                                     "sigma": float(sig), "pull_vs_exact": (float(res) - exact) / float(sig)}
+    return out
 
 
 def batched_run(dev, n_iter=5):

@@ -228,3 +228,28 @@ def test_seed_reproducible():
         inst.compile(integrands.symgauss())
         out.append(inst.run_integration(3))
     np.testing.assert_allclose(out[0], out[1], rtol=1e-12)
+
+
+def test_user_histograms():
+    """run_integration(histograms=...) (monte_carlo.py:645-741), as in the
+    reference's examples/histogram_ex.py: the integrand fills a 2-bin histogram
+    of x_3 weighted by w f; after the run it holds the 1/sigma^2-weighted
+    average of the per-iteration histograms, whose bins add up to the integral
+    and split it in half for the symmetric Gaussian."""
+    from vegasflow_gb300.utils import consume_array_into_indices
+
+    hist = torch.zeros(2, dtype=torch.float64, device="cuda")
+
+    def integrand(xarr, weight=None):
+        f = example_integrand(xarr)
+        idx = torch.clamp((xarr[:, 2] * 2).to(torch.int32), 0, 1).reshape(-1, 1)
+        hist.add_(consume_array_into_indices(f * weight, idx, 2))
+        return f
+
+    inst = PlainFlow(3, int(1e5), verbose=False, seed=31)
+    inst.compile(integrand, check=False)
+    res, sigma = inst.run_integration(5, histograms=(hist,))
+    h = hist.cpu().numpy()
+    assert abs(h.sum() - res) < 1e-6 * abs(res)
+    np.testing.assert_allclose(h, [res / 2, res / 2], atol=5 * sigma)
+    assert len(inst.history) == 5 and all(len(e[2]) == 1 for e in inst.history)

@@ -13,6 +13,7 @@
 #include "vf_internal.h"
 #include "vf_iter.cuh"
 #include "vf_sample.cuh"
+#include "vf_map_f32.cuh"
 #include "vf_vegas_f32.cuh"
 
 namespace {
@@ -213,6 +214,7 @@ int vf_preload(void) {
       load(vf::vegas_f32_kernel(d, integ, 256));
       load(vf::vegas_f32_kernel(d, integ, 128));
     }
+  for (int d = 1; d <= VF_MAX_DIM; ++d) load(vf::vegas_f32_map_kernel(d));
   for (int dmax : {4, 8, 16})
     for (int integ = VF_INT_NONE; integ <= VF_INT_SUM; ++integ) {
       load(vf::sample_kernel_f64(dmax, integ));
@@ -305,6 +307,9 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
   if (rows < 1) rows = 1;
   const bool taps = ind_out || x_out || w_out || f_out;
   const bool fast = !jit && use_vegas_f32(alg, precision, integrand, taps);
+  // the fp32 VEGAS map alone (no integrand, Philox uniforms): x, w, indices to HBM
+  const bool map_only = !jit && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS && integrand == VF_INT_NONE &&
+                        !u_inj && !f_out && (x_out || w_out || ind_out);
   const int threads = fast ? g_f32_threads.load() : VF_THREADS;
   const void* k = jit ? nullptr
                       : (fast ? vf::vegas_f32_kernel(n_dim, integrand, threads)
@@ -337,6 +342,24 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
   a.rows_total = rows;
   a.call_dev = call_dev;
   fill_philox(a, seed, call_ctr);
+  if (map_only) {
+    const void* km = vf::vegas_f32_map_kernel(n_dim);
+    if (!km) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no map kernel for n_dim=%d", n_dim);
+    const int smem_m = vf::vegas_f32_map_smem_bytes(n_dim, VF_THREADS, ind_out != nullptr);
+    int rc = prepare_smem(km, smem_m);
+    if (rc) return rc;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, km, VF_THREADS, smem_m) != cudaSuccess || per_sm < 1)
+      return fail(VF_ERR_CUDA, "vf_sample: occupancy query for the map kernel failed");
+    const long long tiles = (n_events + VF_MAP_EPT * VF_THREADS - 1) / (VF_MAP_EPT * VF_THREADS);
+    long long blocks_m = (long long)per_sm * sm_count();
+    if (tiles < blocks_m) blocks_m = tiles > 0 ? tiles : 1;
+    void* args[] = {&a};
+    const cudaError_t e =
+        cudaLaunchKernel(km, dim3((unsigned)blocks_m), dim3(VF_THREADS), args, smem_m, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "vf_sample launch: %s", cudaGetErrorString(e));
+    return check_launch("vf_sample (map)");
+  }
   if (jit) {
     if (taps && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS)
       return fail(VF_ERR_UNSUPPORTED, "vf_sample: a JIT fp32 VEGAS integrand has no per-event taps");

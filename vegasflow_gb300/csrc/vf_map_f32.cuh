@@ -1,0 +1,153 @@
+// The fp32 VEGAS map without an integrand: the sampler API
+// (generate_random_array, monte_carlo.py:229-275; vflow.py:93-126) and the
+// sampling half of a torch-evaluated iteration.  Per event the same draw as the
+// fused sampler -- ceil(D/4) Philox blocks, the exact integer bin/fraction map,
+// one FMA through the staged per-bin table -- and the event's x (D floats),
+// weight w (float) and, when asked, bin indices (D int32) go to HBM.
+//
+// The stores are the whole cost (36 bytes per event at D = 8 for x and w), so
+// they are staged: each thread writes its events' rows into a shared-memory
+// tile of VF_MAP_EPT x THREADS events, and one thread hands each full tile to the bulk-copy
+// engine (cp.async.bulk shared -> global, contiguous, 16-byte aligned), two
+// tiles in flight.  A thread's own row stores would cost a warp 32 separate
+// 32-byte segments per dimension; a tile is one contiguous transfer.  The last
+// partial tile, and arrays that are not 16-byte aligned, use plain stores.
+#pragma once
+#include "vf_vegas_f32.cuh"
+
+namespace vf {
+
+// events per thread per tile
+#define VF_MAP_EPT 2
+
+__host__ __device__ inline int vegas_f32_map_smem_bytes(int D, int threads, bool with_ind) {
+  const int stage = VF_MAP_EPT * threads * (D * 4 * (with_ind ? 2 : 1) + 4);
+  return D * VF_BINS * 8 + 2 * stage + 128;
+}
+
+__device__ __forceinline__ void bulk_store(void* gdst, u32 ssrc, u32 bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(ssrc), "r"(bytes)
+               : "memory");
+}
+
+template <int D, int THREADS = VF_THREADS>
+__global__ void __launch_bounds__(THREADS, VF_F32_MIN_BLOCKS * VF_THREADS / THREADS)
+vf_vegas_f32_map_kernel(const __grid_constant__ SampleArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NB = D * VF_BINS;
+  float2* cells = reinterpret_cast<float2*>(smem);
+  const int tid = threadIdx.x;
+  const bool limits = a.xmin != nullptr;
+  const CallWords cw = call_words(a);
+  float* x_out = static_cast<float*>(a.x_out);
+  float* w_out = static_cast<float*>(a.w_out);
+  int* ind_out = a.ind_out;
+
+  // ---- the weight constant 50^D * xjac, and the per-bin table {c0, c1}:
+  // x = c0 + c1 m, c0 = xmin + (lo - delta) xdelta, c1 = delta xdelta
+  __shared__ float g_wscale;
+  if (tid == 0) {
+    double ws = a.xjac;
+    for (int d = 0; d < D; ++d) ws *= 50.0;
+    g_wscale = (float)ws;
+  }
+  for (int k = tid; k < NB; k += blockDim.x) {
+    const int d = k / VF_BINS, b = k - d * VF_BINS;
+    const double lo = a.grid[d * VF_EDGES + b];
+    const double dl = a.grid[d * VF_EDGES + b + 1] - lo;
+    double c0 = lo - dl, c1 = dl;
+    if (limits) {
+      c0 = a.xmin[d] + c0 * a.xdelta[d];
+      c1 = c1 * a.xdelta[d];
+    }
+    cells[k] = make_float2((float)c0, (float)c1);
+  }
+  __syncthreads();
+  const float wscale = g_wscale;
+
+  // ---- staging tiles of T = VF_MAP_EPT * THREADS events:
+  // [x: T*D floats][ind: T*D ints][w: T floats], two of them
+  const bool want_ind = ind_out != nullptr;
+  constexpr int T = VF_MAP_EPT * THREADS;
+  constexpr u32 XB = T * D * 4, WB = T * 4;
+  const u32 stage_bytes = XB * (want_ind ? 2u : 1u) + WB;
+  unsigned char* stage0 = smem + ((NB * 8 + 15) & ~15);
+  const bool aligned = ((reinterpret_cast<size_t>(x_out) | reinterpret_cast<size_t>(w_out) |
+                         reinterpret_cast<size_t>(ind_out)) & 15) == 0;
+  const long long n = a.n_events;
+  const long long n_tiles = (n + T - 1) / T;
+  int it = 0;
+  for (long long t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+    const long long e0 = t * T;
+    const bool full = aligned && e0 + T <= n;
+    unsigned char* st = stage0 + (it & 1) * stage_bytes;
+    float* xs = reinterpret_cast<float*>(st);
+    int* is = reinterpret_cast<int*>(st + XB);
+    float* wsm = reinterpret_cast<float*>(st + XB * (want_ind ? 2 : 1));
+    if (full) {
+      // the stage's previous tile (two tiles back) must have been read out
+      if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+      __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < VF_MAP_EPT; ++k) {
+      const int r = k * THREADS + tid;  // row in the tile
+      const long long e = e0 + r;
+      if (e < n) {
+        const u64 ev = (u64)(a.ev_offset + e);
+        float wf = 1.0f;
+        float xr[D];
+        int br[D];
+#pragma unroll
+        for (int q = 0; q < (D + 3) / 4; ++q) {
+          u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = cw.c2base | (u32)q, c3 = cw.c3;
+          philox4x32_10_rk(c0, c1, c2, c3, a.rk);
+          const u32 wq[4] = {c0, c1, c2, c3};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int d = 4 * q + j;
+            if (d < D) {
+              const u64 pp = (u64)(~wq[j]) * 50ull + 25ull;
+              const int i = (int)(pp >> 32);
+              const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
+              const float2 c = cells[d * VF_BINS + i];
+              xr[d] = fmaf(c.y, m, c.x);
+              wf = (d == 0) ? c.y : wf * c.y;
+              br[d] = i;
+            }
+          }
+        }
+        const float w = wf * wscale;
+        if (full) {
+#pragma unroll
+          for (int d = 0; d < D; ++d) xs[r * D + d] = xr[d];
+          if (want_ind)
+#pragma unroll
+            for (int d = 0; d < D; ++d) is[r * D + d] = br[d];
+          wsm[r] = w;
+        } else {
+          if (x_out)
+#pragma unroll
+            for (int d = 0; d < D; ++d) x_out[e * D + d] = xr[d];
+          if (want_ind)
+#pragma unroll
+            for (int d = 0; d < D; ++d) ind_out[e * D + d] = br[d];
+          if (w_out) w_out[e] = w;
+        }
+      }
+    }
+    if (full) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the rows, to the copy engine
+      __syncthreads();
+      if (tid == 0) {
+        if (x_out) bulk_store(x_out + e0 * D, smem_u32(xs), XB);
+        if (want_ind) bulk_store(ind_out + e0 * D, smem_u32(is), XB);
+        if (w_out) bulk_store(w_out + e0, smem_u32(wsm), WB);
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      }
+    }
+  }
+  if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+}  // namespace vf

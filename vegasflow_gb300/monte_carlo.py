@@ -127,6 +127,7 @@ class MonteCarloFlow(ABC):
         self._autotune = bool(autotune)
         self._shape = None
         self._cuda_graph = bool(cuda_graph)
+        self._differentiable = False
         self._graph = None
         self._graph_key = None
 
@@ -357,6 +358,8 @@ class MonteCarloFlow(ABC):
     def run_event(self, tensorize_events=False, **kwargs):
         """Run all events of one iteration; returns the accumulated (res, res2[,
         arr_res2]) as device tensors (monte_carlo.py:420-480)."""
+        if self._differentiable and self._kind == "torch":
+            return self._run_event_autograd()
         want_hist = self._ALG == nat.VF_ALG_VEGAS and self._train_now()
         self._fill_partials(train=want_hist)
         ws = self._history_slot()
@@ -378,12 +381,13 @@ class MonteCarloFlow(ABC):
 
     # ---------------------------------------------------------------- random numbers
     def generate_random_array(self, n_events, *args):
-        """(x, p(x)) for ``n_events`` points (monte_carlo.py:229-247)."""
-        rnds, xjac_raw, *extra = self._generate_random_array(n_events, *args)
+        """(x, p(x)) for ``n_events`` points (monte_carlo.py:229-247): one
+        sampler launch writing x and w (no bin indices) to HBM."""
+        rnds, xjac_raw, *extra = self._generate_random_array(n_events, *args, want_ind=False)
         xjac = xjac_raw / (self.xjac * n_events)
         return rnds, xjac
 
-    def _generate_random_array(self, n_events, *args):
+    def _generate_random_array(self, n_events, *args, want_ind=True):
         """(x, w[, ind]) of ``n_events`` points, weighted as part of an
         ``self.n_events`` iteration (monte_carlo.py:249-275)."""
         self._require_gpu()
@@ -391,7 +395,7 @@ class MonteCarloFlow(ABC):
         x = torch.empty((n, self.n_dim), dtype=self._rdtype, device=self.device)
         w = torch.empty(n, dtype=self._rdtype, device=self.device)
         ind = torch.empty((n, self.n_dim), dtype=torch.int32, device=self.device) \
-            if self._ALG == nat.VF_ALG_VEGAS else None
+            if self._ALG == nat.VF_ALG_VEGAS and want_ind else None
         self._sample(n, 0, self._next_call(), nat.VF_INT_NONE, None, False, False,
                      u_inj=self._injected(n), ind=ind, x=x, w=w)
         if ind is None:
@@ -676,9 +680,53 @@ class MonteCarloFlow(ABC):
                                       "completed; the iteration's sums are incomplete")
 
     def make_differentiable(self):
-        raise NotImplementedError(
-            "make_differentiable: gradients through the GPU sampler are not provided; "
-            "integrate with a torch callable and differentiate its inputs instead")
+        """monte_carlo.py:389-418: returns ``run_event``, whose results then
+        follow torch autograd.  For a torch-callable integrand the events' x and
+        w come from the sampler (they depend on no parameter) and the sums over
+        events are taken by torch, so ``run_event()[0]`` is connected to the
+        integrand's autograd graph: gradients with respect to the integrand's
+        parameters flow through the integral, and each call draws new events.
+        Device integrands have fixed parameters; their results carry no graph."""
+        if self.distribute:
+            raise ValueError("Differentiation is not compatible with distribution")
+        self._differentiable = True
+        if self.event is not None:
+            logger.warning("Recompiling...")
+            self._recompile()
+        return self.run_event
+
+    def _run_event_autograd(self):
+        """run_event for a torch integrand with the sums taken by torch:
+        (res, res2[, arr_res2]) with res and res2 in the autograd graph."""
+        self._require_gpu()
+        vegas = self._ALG == nat.VF_ALG_VEGAS
+        want_hist = vegas and self._train_now()
+        call = self._next_call()
+        res = res2 = hist = None
+        off = 0
+        for nc in _chunk_sizes(self.n_events, self.events_per_run):
+            # fresh buffers: the graph keeps x and w for the backward pass
+            x = torch.empty((nc, self.n_dim), dtype=self._rdtype, device=self.device)
+            w = torch.empty(nc, dtype=self._rdtype, device=self.device)
+            ind = torch.empty((nc, self.n_dim), dtype=torch.int32, device=self.device) if vegas else None
+            self._sample(nc, off, call, nat.VF_INT_NONE, None, False, False, u_inj=self._injected(nc), ind=ind,
+                         x=x, w=w)
+            f = torch.as_tensor(self._tf_integrand(x, weight=w)).to(device=self.device)
+            tmp = (w.reshape(nc, 1) * f.reshape(nc, -1)) if self._vectorial else w * f.reshape(nc)
+            r, r2 = tmp.sum(0), (tmp * tmp).sum(0)
+            res = r if res is None else res + r
+            res2 = r2 if res2 is None else res2 + r2
+            if want_hist:
+                from .utils import consume_array_into_indices
+                main = tmp[:, getattr(self, "_main_dimension", 0)] if self._vectorial else tmp
+                t2 = (main * main).detach().to(torch.float64)
+                h = torch.stack([consume_array_into_indices(t2, ind[:, j:j + 1], BINS_MAX)
+                                 for j in range(self.n_dim)])
+                hist = h if hist is None else hist + h
+            off += nc
+        if want_hist:
+            return res, res2, hist
+        return res, res2
 
     def set_distribute(self, queue_object):
         raise NotImplementedError("dask distribution is not part of the GB300 build (one GPU)")

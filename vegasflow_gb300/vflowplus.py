@@ -12,7 +12,6 @@ for device integrands.
 from __future__ import annotations
 
 import logging
-from functools import partial  # noqa: F401  (kept for API parity of make_differentiable)
 
 import numpy as np
 import torch
@@ -98,9 +97,39 @@ class VegasFlowPlus(VegasFlow):
         super()._can_run_vectorial(expected_shape)
         return False
 
-    def make_differentiable(self):
-        raise NotImplementedError(
-            "make_differentiable: gradients through the GPU sampler are not provided")
+    def _run_event_autograd(self):
+        """(ress, arr_var[, arr_res2]) of one iteration's events with the
+        per-hypercube sums taken by torch (vflowplus.py:187-220), so that they
+        follow the integrand's autograd graph."""
+        self._require_gpu()
+        ws = self._plus_buffers()
+        call = self._next_call()
+        xmin, xdelta, xdj = self._limits_ptrs()
+        n_total = self.n_events
+        u = self._injected(n_total)
+        x = torch.empty((n_total, self.n_dim), dtype=self._rdtype, device=self.device)
+        w = torch.empty(n_total, dtype=self._rdtype, device=self.device)
+        ind = torch.empty((n_total, self.n_dim), dtype=torch.int32, device=self.device)
+        nat.call("vf_plus_sample", self._prec, nat.ptr(self.divisions), self.n_dim, self._n_strat,
+                 self._n_hcubes, nat.ptr(self.n_ev), nat.ptr(self._ev_start), float(self.xjac), xmin,
+                 xdelta, float(xdj), nat.ptr(u), self._seed, call, nat.VF_INT_NONE, None, 0, None,
+                 None, None, self._rows, nat.ptr(ind), nat.ptr(x), nat.ptr(w), nat.ptr(ws["flags"]),
+                 nat.stream_handle())
+        f = torch.as_tensor(self._tf_integrand(x, weight=w)).to(device=self.device).reshape(-1)
+        tmp = w * f
+        n_ev = self.n_ev.to(torch.int64)
+        segm = torch.repeat_interleave(torch.arange(self._n_hcubes, device=self.device), n_ev,
+                                       output_size=n_total)  # vflowplus.py:67 (events laid out by hypercube)
+        zeros = torch.zeros(self._n_hcubes, dtype=tmp.dtype, device=self.device)
+        ress = zeros.index_add(0, segm, tmp)
+        ress2 = zeros.index_add(0, segm, tmp * tmp)
+        arr_var = ress2 * n_ev.to(tmp.dtype) - ress * ress
+        if not self.train:
+            return ress, arr_var
+        from .utils import consume_array_into_indices
+        t2 = (tmp * tmp).detach().to(torch.float64)
+        hist = torch.stack([consume_array_into_indices(t2, ind[:, j:j + 1], BINS_MAX) for j in range(self.n_dim)])
+        return ress, arr_var, hist
 
     # ---------------------------------------------------------------- VEGAS+ steps
     def redistribute_samples(self, arr_var):
@@ -197,6 +226,8 @@ class VegasFlowPlus(VegasFlow):
     def run_event(self, tensorize_events=None, **kwargs):
         """(ress, arr_var, arr_res2) of one iteration's events (vflowplus.py:187-220)
         without updating the grid, the allocation or the running average."""
+        if self._differentiable and self._kind == "torch":
+            return self._run_event_autograd()
         want_hist = bool(self.train)
         self._fill_plus(train=want_hist)
         ws = self._history_slot()
