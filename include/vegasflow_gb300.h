@@ -188,7 +188,8 @@ int vf_plus_reduce_events(int precision, const void* f, const void* w, const int
  * sigma^2 = sum max(var, 0) / (n_ev - 1) with var = ress2 n_ev - ress^2,
  * history/average as vf_iteration_end; when adaptive, redistribute_samples
  * (vflowplus.py:153-163: n_ev = int(max(min_neval, var^(beta/2) N0 / 2 / sum)))
- * and the new ev_start; when train, the grid refinement.
+ * and the new ev_start; when train, the grid refinement (train = 1 in float64,
+ * 2 in float32, as vf_iteration_end).  At most 16384 hypercubes.
  */
 int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, long long* ev_start,
                           int n_hcubes, int adaptive, int min_neval, double init_calls,

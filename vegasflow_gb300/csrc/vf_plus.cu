@@ -166,6 +166,9 @@ int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, lo
   if ((train || hist_out) && (!partials || rows < 1)) return err(VF_ERR_ARG, "vf_plus_iteration_end: partials");
   if (train && !grid) return err(VF_ERR_ARG, "vf_plus_iteration_end: grid required when train");
   if (adaptive && min_neval < 1) return err(VF_ERR_ARG, "vf_plus_iteration_end: min_neval");
+  if (n_hcubes > VF_PEND_CLUSTER * VF_PEND_THREADS * VF_PEND_MAXC)
+    return err(VF_ERR_UNSUPPORTED, "vf_plus_iteration_end: more than 16384 hypercubes");
+  if (train < 0 || train > 2) return err(VF_ERR_ARG, "vf_plus_iteration_end: train must be 0, 1 or 2");
   vf::PlusEndArgs a;
   a.ress = ress;
   a.ress2 = ress2;
@@ -186,10 +189,10 @@ int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, lo
   a.adaptive = adaptive ? 1 : 0;
   a.rows = rows;
   a.n_dim = n_dim;
-  a.train = train ? 1 : 0;
+  a.train = train;
   a.iter = iter;
-  const int blocks = (a.train || hist_out) ? n_dim + 1 : 1;
-  vf::vf_plus_iteration_end_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(a);
+  const int clusters = (a.train || hist_out) ? n_dim + 1 : 1;
+  vf::vf_plus_iteration_end_kernel<<<clusters * VF_PEND_CLUSTER, VF_PEND_THREADS, 0, (cudaStream_t)stream>>>(a);
   return launched("vf_plus_iteration_end");
 }
 

@@ -11,6 +11,8 @@
 #include "vf_refine.cuh"
 #include "vf_sample.cuh"
 
+#include <cooperative_groups.h>
+
 namespace vf {
 
 struct PlusArgs {
@@ -285,96 +287,208 @@ struct PlusEndArgs {
   int iter;
 };
 
-__global__ void __launch_bounds__(256) vf_plus_iteration_end_kernel(const PlusEndArgs a) {
-  const int t = threadIdx.x;
+// var^(beta/2), vflowplus.py:157.  For the default beta = 3/4 the power 3/8 is
+// ((v^(1/2))^(1/2))^(1/2) cubed: three correctly rounded square roots and two
+// products, about a third of the float64 instructions of pow (this part issues
+// one float64 warp instruction per 64 cycles).  NaN for v < 0, as pow.
+__device__ __forceinline__ double plus_damp(double v, double beta) {
+  if (beta == 0.75) {
+    const double r = sqrt(sqrt(sqrt(v)));
+    return r * r * r;
+  }
+  return pow(v, beta / 2.0);
+}
+
+#define VF_PEND_CLUSTER 8
+#define VF_PEND_THREADS 512
+#define VF_PEND_MAXC 4  // hypercubes per thread: up to 8 x 512 x 4 = 16384
+
+// The VEGAS+ iteration end, in clusters of 8 blocks.  Cluster d < D sums
+// dimension d's histogram columns (each block 1/8 of the rows, combined in rank
+// order through distributed shared memory) and refines the grid row.  The last
+// cluster owns the hypercubes: each block a contiguous eighth, each thread a
+// contiguous run of at most VF_PEND_MAXC; it forms var, the sums for res and
+// sigma and the damped variances (fixed-order block and cluster reductions),
+// block 0 records the iteration, and -- adaptive -- every thread turns its damped
+// variances into new counts, followed by an exclusive prefix sum over threads,
+// blocks (through distributed shared memory) and hypercubes into ev_start.
+__global__ void __cluster_dims__(VF_PEND_CLUSTER, 1, 1) __launch_bounds__(VF_PEND_THREADS)
+vf_plus_iteration_end_kernel(const PlusEndArgs a) {
+  namespace cg = cooperative_groups;
+  const cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int group = blockIdx.x / VF_PEND_CLUSTER;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int D = a.n_dim;
   const int H = a.n_hcubes;
-  const int W = 2 + VF_BINS * D;
+  const long long W = 2 + VF_BINS * D;
+  __shared__ double mine[VF_BINS];
   __shared__ double hsm[VF_BINS];
-  if ((a.train || a.hist_out) && (int)blockIdx.x < D) {
-    const int d = blockIdx.x;
-    const double* col0 = a.partials + 2 + d * VF_BINS;
-    sum_hist_columns<5>([=](int r) { return col0 + (long long)r * W; }, a.rows, hsm,
-                        a.hist_out ? a.hist_out + d * VF_BINS : nullptr);
-    if (a.train) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
+  if ((a.train || a.hist_out) && group < D) {
+    const int d = group;
+    const int lo = (int)((long long)a.rows * rank / VF_PEND_CLUSTER);
+    const int hi = (int)((long long)a.rows * (rank + 1) / VF_PEND_CLUSTER);
+    const double* col0 = a.partials + 2 + d * VF_BINS + lo * W;
+    sum_hist_columns<VF_PEND_THREADS / VF_BINS>([=](int r) { return col0 + r * W; }, hi - lo, mine, nullptr);
+    cluster.sync();
+    if (rank == 0 && t < VF_BINS) {
+      double v = mine[t];
+      for (int r = 1; r < VF_PEND_CLUSTER; ++r) v += cluster.map_shared_rank(mine, r)[t];
+      hsm[t] = v;
+      if (a.hist_out) a.hist_out[d * VF_BINS + t] = v;
+    }
+    cluster.sync();
+    if (rank == 0 && a.train == 1) refine_dimension(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
+    if (rank == 0 && a.train == 2) refine_dimension_f32(hsm, a.grid + d * VF_EDGES, a.alpha, a.flags);
     return;
   }
-  __shared__ double red[3][256];
-  __shared__ double s_sum_damped;
-  __shared__ double s_mean;
-  __shared__ long long scan[256];
-  // res = sum ress, sigma^2 = sum max(var, 0) / (n_ev - 1)   (vflowplus.py:230-233)
+
+  // ---- the hypercubes of this block, a contiguous run per thread
+  const int lo = (int)((long long)H * rank / VF_PEND_CLUSTER);
+  const int hi = (int)((long long)H * (rank + 1) / VF_PEND_CLUSTER);
+  const int C = (hi - lo + VF_PEND_THREADS - 1) / VF_PEND_THREADS;
+  const int h0 = lo + t * C;
+  double dmp[VF_PEND_MAXC];
   double r1 = 0.0, r2 = 0.0, r3 = 0.0;
-  for (int h = t; h < H; h += blockDim.x) {
-    const double nev = (double)a.n_ev[h];
-    const double var = __dsub_rn(__dmul_rn(a.ress2[h], nev), __dmul_rn(a.ress[h], a.ress[h]));
-    if (a.arr_var) a.arr_var[h] = var;
-    r1 += a.ress[h];
-    r2 += fmax(var, 0.0) / (nev - 1.0);
-    if (a.adaptive) r3 += pow(var, a.beta / 2.0);  // NaN for var < 0, as the reference
-  }
-  red[0][t] = r1;
-  red[1][t] = r2;
-  red[2][t] = r3;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (t < o) {
-      red[0][t] += red[0][t + o];
-      red[1][t] += red[1][t + o];
-      red[2][t] += red[2][t + o];
+#pragma unroll
+  for (int j = 0; j < VF_PEND_MAXC; ++j) {
+    dmp[j] = 0.0;
+    const int h = h0 + j;
+    if (j < C && h < hi) {
+      // vflowplus.py:216-217, 230-233
+      const double nev = (double)a.n_ev[h];
+      const double var = __dsub_rn(__dmul_rn(a.ress2[h], nev), __dmul_rn(a.ress[h], a.ress[h]));
+      if (a.arr_var) a.arr_var[h] = var;
+      r1 += a.ress[h];
+      r2 += fmax(var, 0.0) / (nev - 1.0);
+      if (a.adaptive) {
+        dmp[j] = plus_damp(var, a.beta);
+        r3 += dmp[j];
+      }
     }
-    __syncthreads();
   }
-  if (t == 0) {
-    const double res = red[0][0];
-    const double sigma = sqrt(red[1][0]);
-    double* hrow = a.history + (long long)a.iter * 2;
-    hrow[0] = res;
-    hrow[1] = sigma;
-    const double wgt = 1.0 / __dmul_rn(sigma, sigma);
-    a.avg[0] = __dadd_rn(a.avg[0], __dmul_rn(res, wgt));
-    a.avg[1] = __dadd_rn(a.avg[1], wgt);
-    const double mean = a.avg[0] / a.avg[1];
-    a.avg[2] = mean;
-    a.avg[3] = sqrt(1.0 / a.avg[1]);
-    s_mean = mean;
-    if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
-    s_sum_damped = red[2][0];
+  __shared__ double wpart[3][VF_PEND_THREADS / 32];
+  __shared__ double tot[3];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    r1 += __shfl_xor_sync(0xffffffffu, r1, o);
+    r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    r3 += __shfl_xor_sync(0xffffffffu, r3, o);
+  }
+  if (lane == 0) {
+    wpart[0][warp] = r1;
+    wpart[1][warp] = r2;
+    wpart[2][warp] = r3;
   }
   __syncthreads();
-  {
+  if (t == 0) {
+    double b1 = 0.0, b2 = 0.0, b3 = 0.0;
+    for (int w = 0; w < VF_PEND_THREADS / 32; ++w) {
+      b1 += wpart[0][w];
+      b2 += wpart[1][w];
+      b3 += wpart[2][w];
+    }
+    tot[0] = b1;
+    tot[1] = b2;
+    tot[2] = b3;
+  }
+  cluster.sync();
+  __shared__ double all[3];  // the cluster's totals, added in rank order in every block
+  __shared__ double s_mean;
+  if (t == 0) {
+    double c1 = 0.0, c2 = 0.0, c3 = 0.0;
+    for (int r = 0; r < VF_PEND_CLUSTER; ++r) {
+      const double* tr = cluster.map_shared_rank(tot, r);
+      c1 += tr[0];
+      c2 += tr[1];
+      c3 += tr[2];
+    }
+    all[0] = c1;
+    all[1] = c2;
+    all[2] = c3;
+    if (rank == 0) {
+      const double res = c1;
+      const double sigma = sqrt(c2);
+      double* hrow = a.history + (long long)a.iter * 2;
+      hrow[0] = res;
+      hrow[1] = sigma;
+      const double wgt = 1.0 / __dmul_rn(sigma, sigma);
+      a.avg[0] = __dadd_rn(a.avg[0], __dmul_rn(res, wgt));
+      a.avg[1] = __dadd_rn(a.avg[1], wgt);
+      const double mean = a.avg[0] / a.avg[1];
+      a.avg[2] = mean;
+      a.avg[3] = sqrt(1.0 / a.avg[1]);
+      s_mean = mean;
+      if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+    }
+  }
+  __syncthreads();
+  if (rank == 0) {
     const double chi2 = block_chi2(a.history, 2, 1, a.iter + 1, s_mean);
     if (t == 0) a.avg[4] = a.iter > 0 ? chi2 / a.iter : 0.0;
   }
-  if (!a.adaptive) return;
-  // vflowplus.py:157-163: n_ev = int(max(min_neval, d^(beta/2) N0 / 2 / sum d))
-  const double sum_d = s_sum_damped;
-  // new counts, then an exclusive prefix sum in chunks of blockDim
-  long long carry = 0;
-  for (int base = 0; base < H; base += blockDim.x) {
-    const int h = base + t;
-    long long v = 0;
-    if (h < H) {
-      double var = __dsub_rn(__dmul_rn(a.ress2[h], (double)a.n_ev[h]), __dmul_rn(a.ress[h], a.ress[h]));
-      const double dmp = pow(var, a.beta / 2.0);
-      const double nn = fmax((double)a.min_neval, dmp * a.init_calls / 2.0 / sum_d);
-      v = (long long)(int)nn;
-    }
-    __syncthreads();  // everyone has read n_ev[h] before it is rewritten
-    if (h < H) a.n_ev[h] = (int)v;
-    scan[t] = v;
-    __syncthreads();
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {  // inclusive Hillis-Steele scan
-      const long long add = t >= o ? scan[t - o] : 0;
-      __syncthreads();
-      scan[t] += add;
-      __syncthreads();
-    }
-    if (h < H) a.ev_start[h] = carry + scan[t] - v;
-    carry += scan[blockDim.x - 1];
-    __syncthreads();
+  if (!a.adaptive) {
+    cluster.sync();  // the other blocks' totals stay readable until every block has read them
+    return;
   }
-  if (t == 0) a.ev_start[H] = carry;
+
+  // ---- reallocation, vflowplus.py:157-163: n_ev = int(max(min_neval, d N0 / 2 / sum d))
+  const double sum_d = all[2];
+  long long cnt[VF_PEND_MAXC];
+  long long own = 0;
+#pragma unroll
+  for (int j = 0; j < VF_PEND_MAXC; ++j) {
+    cnt[j] = 0;
+    if (j < C && h0 + j < hi) {
+      const double nn = fmax((double)a.min_neval, dmp[j] * a.init_calls / 2.0 / sum_d);
+      cnt[j] = (long long)(int)nn;
+      own += cnt[j];
+    }
+  }
+  // exclusive prefix of `own` over the block's threads (thread order = hypercube order)
+  long long inc = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  __shared__ long long wsum[VF_PEND_THREADS / 32];
+  __shared__ long long btot;
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (t == 0) {
+    long long acc = 0;
+    for (int w = 0; w < VF_PEND_THREADS / 32; ++w) {
+      const long long v = wsum[w];
+      wsum[w] = acc;
+      acc += v;
+    }
+    btot = acc;
+  }
+  cluster.sync();  // every block's total is ready
+  __shared__ long long boff;
+  if (t == 0) {
+    long long off = 0, all_ev = 0;
+    for (int r = 0; r < VF_PEND_CLUSTER; ++r) {
+      const long long v = *cluster.map_shared_rank(&btot, r);
+      if (r < rank) off += v;
+      all_ev += v;
+    }
+    boff = off;
+    if (rank == 0) a.ev_start[H] = all_ev;
+  }
+  __syncthreads();
+  long long e = boff + wsum[warp] + inc - own;
+#pragma unroll
+  for (int j = 0; j < VF_PEND_MAXC; ++j) {
+    const int h = h0 + j;
+    if (j < C && h < hi) {
+      a.n_ev[h] = (int)cnt[j];
+      a.ev_start[h] = e;
+      e += cnt[j];
+    }
+  }
+  cluster.sync();  // the distributed reads above are done before any block exits
 }
 
 }  // namespace vf

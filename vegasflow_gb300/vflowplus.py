@@ -205,7 +205,8 @@ class VegasFlowPlus(VegasFlow):
         ws = self._plus_buffers()
         nat.call("vf_plus_iteration_end", nat.ptr(ws["ress"]), nat.ptr(ws["ress2"]), nat.ptr(self.n_ev),
                  nat.ptr(self._ev_start), self._n_hcubes, int(self._adaptive), int(self.min_neval_hcube),
-                 float(self._init_calls), nat.ptr(ws["partials"]), self._rows, self.n_dim, int(bool(train)),
+                 float(self._init_calls), nat.ptr(ws["partials"]), self._rows, self.n_dim,
+                 (2 if self._prec == nat.VF_PREC_F32 else 1) if train else 0,  # fp32: float32 refinement
                  float(ALPHA), float(BETA), nat.ptr(self.divisions),
                  nat.ptr(ws["hist"]) if want_hist else None, nat.ptr(ws["arr_var"]), nat.ptr(ws["history"]),
                  nat.ptr(ws["avg"]), int(self._it), nat.ptr(ws["flags"]), nat.stream_handle())
