@@ -22,6 +22,10 @@ inline const void* vegas_f32_kernel(int n_dim, int integrand, int threads = 256)
   return n_dim <= 8 ? vegas_f32_kernel_a256(n_dim, integrand) : vegas_f32_kernel_b256(n_dim, integrand);
 }
 
+// The fp32 VEGAS+ sampler for built-in integrands, specialised on the
+// dimension count (Philox uniforms; 256 threads per block).
+const void* plus_f32_kernel(int n_dim, int integrand);
+
 // The fp32 VEGAS map kernel without an integrand (x, w, bin indices to HBM),
 // specialised on the dimension count; 256 threads per block.
 const void* vegas_f32_map_kernel(int n_dim);

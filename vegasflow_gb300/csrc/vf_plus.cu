@@ -7,6 +7,7 @@
 #include "vegasflow_gb300.h"
 #include "vf_internal.h"
 #include "vf_plus.cuh"
+#include "vf_plus_f32.cuh"
 
 namespace {
 
@@ -87,7 +88,10 @@ int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, in
     return err(VF_ERR_ARG, "vf_plus_sample: ress/ress2/partials required when evaluating");
   if ((integrand == VF_INT_SYMGAUSS || integrand == VF_INT_GAUSS || integrand == VF_INT_BREIT_WIGNER) && !params)
     return err(VF_ERR_ARG, "vf_plus_sample: integrand needs params");
-  const void* k = plus_kernel(precision, n_dim, integrand);
+  // fp32 with a built-in integrand and Philox uniforms: the float32 kernel
+  const bool f32 = precision == VF_PREC_F32 && integrand >= VF_INT_SYMGAUSS && integrand <= VF_INT_SUM &&
+                   !u_inj && !ind_out && !x_out && !w_out;
+  const void* k = f32 ? vf::plus_f32_kernel(n_dim, integrand) : plus_kernel(precision, n_dim, integrand);
   if (!k) return err(VF_ERR_UNSUPPORTED, "vf_plus_sample: no kernel");
   vf::PlusArgs a;
   a.grid = grid;
@@ -119,7 +123,8 @@ int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, in
   }
   for (int q = 0; q < 8; ++q) a.ctr2[q] = (call_ctr << 4) | (unsigned int)q;
   a.ctr3 = call_ctr >> 28;
-  const int smem = vf::plus_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, a.train);
+  const int smem = f32 ? vf::plus_f32_smem_bytes(n_dim, a.train)
+                       : vf::plus_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, a.train);
   void* args[] = {&a};
   const cudaError_t e = cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return err(VF_ERR_LAUNCH, cudaGetErrorString(e));
@@ -210,6 +215,11 @@ cudaError_t preload_plus_kernels() {
           if (e != cudaSuccess) return e;
         }
       }
+  for (int d = 1; d <= VF_MAX_DIM; ++d)
+    for (int integ = VF_INT_SYMGAUSS; integ <= VF_INT_SUM; ++integ) {
+      const cudaError_t e = cudaFuncGetAttributes(&attr, plus_f32_kernel(d, integ));
+      if (e != cudaSuccess) return e;
+    }
   cudaError_t e = cudaFuncGetAttributes(&attr, vf_plus_reduce_kernel<double>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_plus_reduce_kernel<float>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_plus_iteration_end_kernel);

@@ -8,42 +8,13 @@
 // Hypercube h has coordinates p_d = digit d of h in base n_strat, the last
 // dimension fastest (the itertools.product order of vflowplus.py:126-128).
 #pragma once
+#include "vf_plus_args.cuh"
 #include "vf_refine.cuh"
 #include "vf_sample.cuh"
 
 #include <cooperative_groups.h>
 
 namespace vf {
-
-struct PlusArgs {
-  const double* grid;        // [D][51]
-  const int* n_ev;           // [H]
-  const long long* ev_start; // [H + 1]
-  const double* xmin;        // nullable [D]
-  const double* xdelta;      // nullable [D]
-  const double* u_inj;       // nullable [n_events][D] (post-affine uniforms, event order)
-  const double* params;
-  double* ress;              // [H]: sum of w f per hypercube (nullable when sampling only)
-  double* ress2;             // [H]: sum of (w f)^2
-  double* partials;          // [rows][2 + 50 D]: block sums and histogram
-  int* ind_out;              // nullable taps, indexed by event
-  void* x_out;
-  void* w_out;
-  int* flags;
-  double xjac;               // 1 / n_hypercubes (vflowplus.py:139, :144-146)
-  double xdeltajac;
-  int n_dim;
-  int n_strat;
-  int n_hcubes;
-  int train;
-  RoundKeys rk;
-  unsigned int ctr2[8];
-  unsigned int ctr3;
-};
-
-__host__ __device__ inline int plus_smem_bytes(int real_size, int D, int train) {
-  return D * VF_EDGES * 8 + (train ? D * VF_BINS * real_size : 0) + 2 * VF_MAX_DIM * 8;
-}
 
 template <typename Real, int DMAX, int INTEG>
 __global__ void __launch_bounds__(VF_THREADS) vf_plus_kernel(const PlusArgs a) {

@@ -1,0 +1,37 @@
+// The argument block of the VEGAS+ samplers (float64 and fp32 kernels).
+#pragma once
+#include "vf_sample.cuh"
+
+namespace vf {
+
+struct PlusArgs {
+  const double* grid;        // [D][51]
+  const int* n_ev;           // [H]
+  const long long* ev_start; // [H + 1]
+  const double* xmin;        // nullable [D]
+  const double* xdelta;      // nullable [D]
+  const double* u_inj;       // nullable [n_events][D] (post-affine uniforms, event order)
+  const double* params;
+  double* ress;              // [H]: sum of w f per hypercube (nullable when sampling only)
+  double* ress2;             // [H]: sum of (w f)^2
+  double* partials;          // [rows][2 + 50 D]: block sums and histogram
+  int* ind_out;              // nullable taps, indexed by event
+  void* x_out;
+  void* w_out;
+  int* flags;
+  double xjac;               // 1 / n_hypercubes (vflowplus.py:139, :144-146)
+  double xdeltajac;
+  int n_dim;
+  int n_strat;
+  int n_hcubes;
+  int train;
+  RoundKeys rk;
+  unsigned int ctr2[8];
+  unsigned int ctr3;
+};
+
+__host__ __device__ inline int plus_smem_bytes(int real_size, int D, int train) {
+  return D * VF_EDGES * 8 + (train ? D * VF_BINS * real_size : 0) + 2 * VF_MAX_DIM * 8;
+}
+
+}  // namespace vf
