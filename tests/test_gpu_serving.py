@@ -71,3 +71,88 @@ def test_short_realtime_run():
     assert m["requests"] == len(reqs) and m["flags"] == 0
     assert 0 < m["p50_latency_s"] <= m["p99_latency_s"] < 30.0
     assert m["events_per_s"] > 1e8
+
+
+def _drive(server, steps, now=0.0):
+    """Advance the server by hand: triage, admission, one step each."""
+    for _ in range(steps):
+        server._triage(now)
+        server._admit(now)
+        if server.active:
+            server.step(lambda: now)
+
+
+def test_rejections_do_not_stop_the_server():
+    server = VegasServer(max_slots=64, hbm_budget=2e7, seed=3)
+    good = Request(3, 50_000, integrands.symgauss(0.2), target_rel_sigma=1e-9, max_iterations=3, rid=0)
+    bad = [Request(17, 1000, integrands.symgauss(), rid=1),                                   # dimensions
+           Request(2, 1, integrands.symgauss(), rid=2),                                       # events
+           Request(4, 1000, integrands.cuda_integrand("__device__ vf_real f(const vf_real* x, int n, "
+                                                     "vf_real w, const double* p) { return x[0]; }",
+                                                     "f"), rid=3),                            # not built in
+           Request(3, 1000, integrands.gauss([0.5, 0.5], [0.1, 0.1]), rid=4),                 # params for 2-D
+           Request(16, 10 ** 9, integrands.symgauss(), rid=5)]                               # over the budget
+    assert server.submit(good)
+    for r in bad:
+        assert not server.submit(r)
+        assert r.status == "rejected" and r.error
+    _drive(server, 4)
+    assert good.status == "finished" and good.iterations == 3
+
+
+def test_cancel_waiting_and_active():
+    server = VegasServer(max_slots=2, hbm_budget=1e9, seed=5)
+    reqs = [Request(4, 100_000, integrands.symgauss(0.2), target_rel_sigma=1e-9, max_iterations=10, rid=i)
+            for i in range(3)]
+    for r in reqs:
+        server.submit(r)
+    _drive(server, 2)  # two slots: requests 0 and 1 active, 2 waiting
+    assert [r.status for r in reqs] == ["active", "active", "waiting"]
+    server.cancel(1)
+    server.cancel(2)
+    _drive(server, 1)
+    assert reqs[1].status == "cancelled" and reqs[2].status == "cancelled"
+    assert reqs[1].iterations == 2 and np.isfinite(reqs[1].result)  # its result so far is kept
+    _drive(server, 10)
+    assert reqs[0].status == "finished" and reqs[0].iterations == 10
+
+
+def test_expiry():
+    server = VegasServer(max_slots=8, hbm_budget=1e9, seed=6)
+    slow = Request(4, 100_000, integrands.symgauss(0.2), target_rel_sigma=1e-9, max_iterations=50, rid=0,
+                   arrival=0.0, timeout=1.0)
+    server.submit(slow)
+    _drive(server, 3, now=0.5)
+    assert slow.status == "active" and slow.iterations == 3
+    _drive(server, 1, now=1.5)
+    assert slow.status == "expired" and slow.iterations == 3 and "timed out" in slow.error
+    assert server.free_slots and server.bytes_in_use == 0
+
+
+def test_allocation_failures_fail_only_their_requests():
+    """Host-side fault injection: an admission whose slot set-up fails, and a
+    partial-row buffer that cannot grow, fail the requests concerned; the
+    others are served."""
+    state = {"admit": 1, "grow": 1}
+
+    def hook(event, **info):
+        if state.get(event, 0) > 0:
+            state[event] -= 1
+            raise MemoryError(f"injected {event} failure")
+
+    server = VegasServer(max_slots=16, hbm_budget=1e9, seed=7, fault_hook=hook)
+    server.partials = server.partials[:200]  # one request's rows (152) fit, two do not
+    first = [Request(3, 20_000, integrands.symgauss(0.2), max_iterations=2, rid=i) for i in range(2)]
+    for r in first:
+        server.submit(r)
+    _drive(server, 1)  # the admission fails
+    assert all(r.status == "failed" and "admission failed" in r.error for r in first)
+    assert server.bytes_in_use == 0 and len(server.free_slots) == 16
+    second = [Request(3, 20_000, integrands.symgauss(0.2), max_iterations=2, rid=10 + i) for i in range(3)]
+    for r in second:
+        server.submit(r)
+    _drive(server, 3)  # the buffer cannot grow: the newest requests fail until the rest fit
+    failed = [r for r in second if r.status == "failed"]
+    served = [r for r in second if r.status in ("converged", "finished")]
+    assert failed and all("allocation failed" in r.error for r in failed)
+    assert len(failed) + len(served) == 3

@@ -13,6 +13,16 @@ and their work overlaps with everyone else's.
 An integral's numbers depend only on itself (its Philox stream id and fixed
 event tiles): a request gives the same result alone and in any mix, up to the
 rounding of the histogram's float atomics.
+
+Failures stay with the request they concern, never the server: a request that
+cannot be served (unsupported integrand or dimension, larger than the whole
+HBM budget) is rejected at submission; a request can be cancelled, or expire
+after its ``timeout``, at the next step boundary; a device allocation that
+fails (growing the partial-row buffer, admitting requests) fails the requests
+it was for and the server carries on with the others.  ``fault_hook``
+(host-side fault injection for tests) is called at those points and may raise.
+Every finished request carries a ``status`` (converged, finished, cancelled,
+expired, rejected, failed) and, for the last three, an ``error``.
 """
 
 from __future__ import annotations
@@ -53,6 +63,9 @@ class Request:
     admitted: float = float("nan")
     finished: float = float("nan")
     slot: int = -1
+    timeout: float = float("inf")  # seconds after arrival
+    status: str = "new"           # waiting, active, then a final status (see the module docstring)
+    error: str = ""
     exact: float = field(default=float("nan"), repr=False)
 
     @property
@@ -124,7 +137,7 @@ class VegasServer:
     stream id)."""
 
     def __init__(self, max_slots=2048, hbm_budget=150e9, tile_events=DEFAULT_TILE_EVENTS, seed=1234,
-                 hist_cap=32, device=None):
+                 hist_cap=32, device=None, fault_hook=None):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
             raise RuntimeError("VegasServer runs on a CUDA device only")
@@ -157,15 +170,84 @@ class VegasServer:
         self.events_done = 0
         self.steps = 0
         self._next_rid = 0
+        self._cancel = set()
+        self.fault_hook = fault_hook
 
     # ---------------------------------------------------------------- admission
-    def submit(self, req: Request):
-        if not isinstance(req.integrand, DeviceIntegrand) or not 1 <= req.n_dim <= MAX_DIM:
-            raise ValueError("requests need a built-in DeviceIntegrand and 1 <= n_dim <= 16")
+    def _fault(self, event, **info):
+        if self.fault_hook is not None:
+            self.fault_hook(event, **info)
+
+    def _finish(self, req, status, now, error=""):
+        """Retire ``req`` with a final status (freeing its slot if it held one)."""
+        if req.slot >= 0:
+            self.free_slots.append(req.slot)
+            self.bytes_in_use -= req._footprint
+            req.slot = -1
+        req.status = status
+        req.error = error
+        req.converged = status == "converged"
+        req.finished = now
+        self.done.append(req)
+
+    def submit(self, req: Request, now=None):
+        """Queue ``req``; a request that can never be served is rejected here
+        (status ``rejected``) instead of raising."""
         if req.rid < 0:
             req.rid = self._next_rid
         self._next_rid = max(self._next_rid, req.rid + 1)
+        now = req.arrival if now is None else now
+        reason = ""
+        integ = req.integrand
+        if not isinstance(integ, DeviceIntegrand) or not nat.VF_INT_SYMGAUSS <= integ.integrand_id <= nat.VF_INT_SUM:
+            reason = "batched serving takes built-in device integrands"
+        elif not 1 <= req.n_dim <= MAX_DIM:
+            reason = f"n_dim={req.n_dim} outside 1..{MAX_DIM}"
+        elif req.n_events < 2:
+            reason = f"n_events={req.n_events} < 2"
+        elif request_footprint(req.n_dim, req.n_events, self.tile_events, self.hist_cap) > self.hbm_budget:
+            reason = "larger than the HBM budget"
+        else:
+            try:
+                integ.check_dims(req.n_dim)
+            except ValueError as exc:
+                reason = str(exc)
+        if reason:
+            self._finish(req, "rejected", now, reason)
+            return False
+        req.status = "waiting"
         self.waiting.append(req)
+        return True
+
+    def cancel(self, rid):
+        """Cancel request ``rid``: a waiting one at once, an active one at the
+        next step boundary (its result so far is kept)."""
+        self._cancel.add(int(rid))
+
+    def _triage(self, now):
+        """Cancellations and expiries, between steps (no expiry without a clock)."""
+
+        def expired(req):
+            return math.isfinite(now) and now >= req.arrival + req.timeout
+
+        keep = []
+        for req in self.waiting:
+            if req.rid in self._cancel:
+                self._finish(req, "cancelled", now, "cancelled before admission")
+            elif expired(req):
+                self._finish(req, "expired", now, "timed out before admission")
+            else:
+                keep.append(req)
+        self.waiting = keep
+        keep = []
+        for req in self.active:
+            if req.rid in self._cancel:
+                self._finish(req, "cancelled", now, "cancelled")
+            elif expired(req):
+                self._finish(req, "expired", now, f"timed out after {req.iterations} iterations")
+            else:
+                keep.append(req)
+        self.active = keep
 
     def _admit(self, now):
         admitted = []
@@ -183,6 +265,20 @@ class VegasServer:
         self.waiting = keep
         if not admitted:
             return
+        try:
+            self._fault("admit", requests=admitted)
+            self._load_slots(admitted)
+        except (RuntimeError, MemoryError) as exc:  # a device allocation failed: fail these requests only
+            for req in admitted:
+                self._finish(req, "failed", now, f"admission failed: {exc}")
+            return
+        for req in admitted:
+            req.status = "active"
+        self.active.extend(admitted)
+
+    def _load_slots(self, admitted):
+        """Initialise the slots of newly admitted requests (uniform grid,
+        parameters, cleared history, average and counters)."""
         slots = torch.as_tensor([r.slot for r in admitted], dtype=torch.int64, device=self.device)
         grid_rows = self.grids.view(self.max_slots, MAX_DIM, BINS_MAX + 1)
         grid_rows[slots] = self._uniform_row
@@ -195,18 +291,32 @@ class VegasServer:
         self.avg[slots] = 0.0
         self.iters[slots] = 0
         self.calls[slots] = 0
-        self.active.extend(admitted)
 
     # ---------------------------------------------------------------- one step
+    def _tables(self, act):
+        return step_tables([r.n_events for r in act], [r.n_dim for r in act], [r.slot for r in act],
+                           [r.rid for r in act], [r.integrand.integrand_id for r in act],
+                           [r.slot * MAX_DIM * (BINS_MAX + 1) for r in act],
+                           [r.slot * PARAMS_PER_SLOT for r in act], self.tile_events)
+
     def step(self, now_fn):
         """Advance every active request by one iteration, then retire finished ones."""
-        act = self.active
-        t = step_tables([r.n_events for r in act], [r.n_dim for r in act], [r.slot for r in act],
-                        [r.rid for r in act], [r.integrand.integrand_id for r in act],
-                        [r.slot * MAX_DIM * (BINS_MAX + 1) for r in act],
-                        [r.slot * PARAMS_PER_SLOT for r in act], self.tile_events)
+        act = list(self.active)
+        t = self._tables(act)
         if t["rows_total"] > self.partials.numel():
-            self.partials = torch.zeros(int(t["rows_total"] * 1.5), dtype=torch.float64, device=self.device)
+            try:
+                self._fault("grow", rows=t["rows_total"])
+                self.partials = torch.zeros(int(t["rows_total"] * 1.5), dtype=torch.float64, device=self.device)
+            except (RuntimeError, MemoryError) as exc:
+                # no room for this step's partial rows: fail the newest requests until the
+                # rest fit the buffer there is, and take the step with those
+                now = now_fn()
+                while act and t["rows_total"] > self.partials.numel():
+                    self._finish(act.pop(), "failed", now, f"device allocation failed: {exc}")
+                    t = self._tables(act)
+                self.active = act
+                if not act:
+                    return
         dev = self.device
         items = torch.from_numpy(t["items"].view(np.uint8)).to(dev, non_blocking=True)
         arrs = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev, non_blocking=True)
@@ -240,11 +350,7 @@ class VegasServer:
             r.result, r.sigma = float(m), float(sg)
             conv = math.isfinite(m) and math.isfinite(sg) and m != 0.0 and sg / abs(m) <= r.target_rel_sigma
             if conv or it >= r.max_iterations:
-                r.converged = bool(conv)
-                r.finished = now
-                self.free_slots.append(r.slot)
-                self.bytes_in_use -= r._footprint
-                self.done.append(r)
+                self._finish(r, "converged" if conv else "finished", now)
             else:
                 still.append(r)
         self.active = still
@@ -265,8 +371,9 @@ class VegasServer:
         while pi < len(pending) or self.waiting or self.active:
             now = now_fn()
             while pi < len(pending) and pending[pi].arrival <= now:
-                self.submit(pending[pi])
+                self.submit(pending[pi], now=now)
                 pi += 1
+            self._triage(now)
             if self.waiting:
                 self._admit(now)
             if not self.active:
@@ -275,8 +382,8 @@ class VegasServer:
                     if wait > 0:
                         time.sleep(min(wait, 0.01))
                     continue
-                if self.waiting:
-                    raise RuntimeError("a waiting request does not fit the HBM budget or the slot pool")
+                if self.waiting:  # every waiting request fits an empty pool: admission retries
+                    continue
                 break
             ts = time.perf_counter()
             self.step(now_fn)
@@ -287,9 +394,14 @@ class VegasServer:
         if not realtime:
             for r in self.done:
                 r.finished = r.arrival  # no clock: latencies are not measured
-        lat = [r.latency for r in self.done]
+        served = [r for r in self.done if r.status in ("converged", "finished")]
+        lat = [r.latency for r in served]
         flags = int(self._flags.item())
+        by_status = {}
+        for r in self.done:
+            by_status[r.status] = by_status.get(r.status, 0) + 1
         return {"requests": len(self.done), "converged": int(sum(r.converged for r in self.done)),
+                "status": by_status,
                 "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99),
                 "mean_latency_s": float(np.mean(lat)) if lat else float("nan"),
                 "events": self.events_done, "wall_s": wall, "busy_s": busy,
