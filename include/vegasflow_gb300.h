@@ -293,6 +293,15 @@ int vf_jit_check(const char* source, const char* func_name, int alg, int precisi
                  int log_size);
 
 /*
+ * Self-test of the device-side bounded wait (no counterpart in the reference):
+ * one block waits, with the same bounded poll loop as the TMA-staged sampler,
+ * on a barrier that nothing completes; after `polls` polls (1..2^20) every
+ * thread gives up and VF_FLAG_TIMEOUT is or-ed into *flag (device memory).
+ * Exercises the timeout path without any fault; the context stays usable.
+ */
+int vf_wait_selftest(int polls, int* flag, void* stream);
+
+/*
  * Load every kernel of the library on the current device now (no counterpart
  * in the reference).  Kernels are otherwise loaded at their first launch; on
  * this platform a kernel loaded after a CUDA graph had been captured in the

@@ -110,3 +110,14 @@ def test_history_full_flag():
     assert counters.tolist() == [1, 1]  # the second call did not advance
     assert int(flags.item()) & nat.VF_FLAG_HISTORY_FULL
     assert history[0, 1].item() > 0
+
+
+def test_nvtx_ranges_do_not_change_results(monkeypatch):
+    """VEGASFLOW_NVTX=1 wraps iterations in NVTX ranges; results are unchanged."""
+    out = []
+    for flag in ("0", "1"):
+        monkeypatch.setenv("VEGASFLOW_NVTX", flag)
+        inst = VegasFlow(3, 50_000, verbose=False, precision="fp64", seed=8)
+        inst.compile(integrands.symgauss())
+        out.append(inst.run_integration(3))
+    np.testing.assert_allclose(out[1], out[0], rtol=1e-12)

@@ -298,3 +298,17 @@ def test_float32_refinement_close_to_float64(spread):
     np.testing.assert_allclose(out[2], want, rtol=0, atol=2e-5)
     assert np.all(np.diff(out[2], axis=1) >= 0)
     assert np.all(out[2][:, 0] == 0.0) and np.all(out[2][:, -1] == 1.0)
+
+
+def test_bounded_device_wait_reports_timeout():
+    """The TMA path's bounded mbarrier wait, on a barrier nothing completes,
+    gives up and sets VF_FLAG_TIMEOUT; the context stays usable afterwards."""
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    lib = nat.load()
+    assert lib.vf_wait_selftest(2000, nat.ptr(flag), nat.stream_handle()) == nat.VF_OK
+    torch.cuda.synchronize()
+    assert int(flag.item()) & nat.VF_FLAG_TIMEOUT
+    inst = VegasFlow(2, 10_000, verbose=False, seed=1)
+    inst.compile(integrands.symgauss())
+    res, sig = inst.run_integration(2)
+    assert np.isfinite(res) and sig > 0

@@ -81,6 +81,7 @@ SIGNATURES = {
     "vf_jit_integrand": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, _P],
     "vf_jit_check": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, ctypes.c_char_p, _I],
     "vf_preload": [],
+    "vf_wait_selftest": [_I, _P, _P],
     "vf_tune_set": [_I, _I],
     "vf_tune_get": [_I, _P],
 }

@@ -4,6 +4,7 @@
 // warp-instruction rate at the clocks of the run.
 #include "vegasflow_gb300.h"
 #include "vf_internal.h"
+#include "vf_vegas_f32.cuh"
 
 #include <cuda_runtime.h>
 
@@ -35,9 +36,35 @@ extern "C" int vf_issue_probe(float* out, int blocks, int iters, long long* fma_
   return cudaGetLastError() == cudaSuccess ? VF_OK : VF_ERR_LAUNCH;
 }
 
+namespace {
+
+// The bounded wait of the TMA path, on a barrier that nothing completes: every
+// thread gives up after `polls` polls and the block reports it.
+__global__ void __launch_bounds__(64) vf_wait_selftest_kernel(int polls, int* flag) {
+  __shared__ alignas(8) unsigned long long bar;
+  const unsigned b = (unsigned)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(b), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool ok = vf::mbar_wait_bounded(b, 0u, polls);
+  if (!__syncthreads_and(ok) && threadIdx.x == 0) atomicOr(flag, VF_FLAG_TIMEOUT);
+}
+
+}  // namespace
+
+extern "C" int vf_wait_selftest(int polls, int* flag, void* stream) {
+  if (!flag || polls < 1 || polls > (1 << 20)) return VF_ERR_ARG;
+  vf_wait_selftest_kernel<<<1, 64, 0, (cudaStream_t)stream>>>(polls, flag);
+  return cudaGetLastError() == cudaSuccess ? VF_OK : VF_ERR_LAUNCH;
+}
+
 namespace vf {
 cudaError_t preload_probe_kernels() {
   cudaFuncAttributes attr;
-  return cudaFuncGetAttributes(&attr, vf_issue_probe_kernel);
+  cudaError_t e = cudaFuncGetAttributes(&attr, vf_issue_probe_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_wait_selftest_kernel);
+  return e;
 }
 }  // namespace vf

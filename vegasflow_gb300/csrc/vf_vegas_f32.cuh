@@ -99,10 +99,10 @@ __device__ __forceinline__ void tma_load_tile(u32 dst, const void* tmap, int x, 
       : "memory");
 }
 
-// Wait for phase `parity` of the barrier, giving up after a bounded number of
-// polls (about a tenth of a second); returns whether the phase completed.
-__device__ __forceinline__ bool mbar_wait_bounded(u32 bar, u32 parity) {
-  for (int i = 0; i < (1 << 20); ++i) {
+// Wait for phase `parity` of the barrier, giving up after `polls` polls (the
+// default is about a tenth of a second); returns whether the phase completed.
+__device__ __forceinline__ bool mbar_wait_bounded(u32 bar, u32 parity, int polls = 1 << 20) {
+  for (int i = 0; i < polls; ++i) {
     u32 ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"

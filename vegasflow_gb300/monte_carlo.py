@@ -49,6 +49,23 @@ from .integrands import DeviceIntegrand
 
 logger = logging.getLogger("vegasflow.monte_carlo")
 
+
+class _nvtx:
+    """An NVTX range (for Nsight timelines) around a block of host calls when
+    VEGASFLOW_NVTX=1; nothing otherwise."""
+
+    def __init__(self, name):
+        self.name = name
+        self.on = os.environ.get("VEGASFLOW_NVTX", "0") == "1"
+
+    def __enter__(self):
+        if self.on:
+            torch.cuda.nvtx.range_push(self.name)
+
+    def __exit__(self, *exc):
+        if self.on:
+            torch.cuda.nvtx.range_pop()
+
 VF_MAX_DIM = 16
 
 
@@ -608,11 +625,13 @@ class MonteCarloFlow(ABC):
         all_results = []
         graph = self._graph_ready(histograms)
         if graph:
-            self._run_graph(n_iter, log_time)
+            with _nvtx(f"vegasflow: {n_iter} graph iterations"):
+                self._run_graph(n_iter, log_time)
         for i in range(0 if graph else n_iter):
             if log_time:
                 start = time.time()
-            res, error = self._run_iteration()
+            with _nvtx(f"vegasflow: iteration {i}"):
+                res, error = self._run_iteration()
             all_results.append((res, error))
             hist_copy = copy.deepcopy(histograms) if histograms else None
             if histograms:
