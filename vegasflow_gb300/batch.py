@@ -64,7 +64,13 @@ class VegasBatch:
         blk_item, blk_role = [], []
         goff = poff = roff = 0
         self.dims, self.events, self.integrands = [], [], []
-        for i, (n_dim, n_events, integ) in enumerate(specs):
+        # integrals with n_dim <= 8 first: their tiles go to the sampler of that
+        # dimension class (smaller shared tables, more blocks per SM); the slot
+        # (result index) stays the integral's position in `specs`
+        order = sorted(range(self.n_items), key=lambda i: int(specs[i][0]) > 8)
+        self._n_low_tiles = 0
+        for pos, i in enumerate(order):  # pos: the integral's place in the items array
+            n_dim, n_events, integ = specs[i]
             n_dim, n_events = int(n_dim), int(n_events)
             if not isinstance(integ, DeviceIntegrand) or not 1 <= integ.integrand_id <= nat.VF_INT_SUM:
                 raise TypeError("batched integrals need a built-in DeviceIntegrand")
@@ -74,10 +80,12 @@ class VegasBatch:
             p = integ.params(n_dim)
             n_tiles = (n_events + self.tile_events - 1) // self.tile_events
             width = 2 + BINS_MAX * n_dim
-            items[i] = (n_events, goff, poff, 1.0 / n_events, n_dim, integ.integrand_id, stream_ids[i],
-                        len(tile_item), n_tiles, int(bool(train)), i, 0)
+            items[pos] = (n_events, goff, poff, 1.0 / n_events, n_dim, integ.integrand_id, stream_ids[i],
+                          len(tile_item), n_tiles, int(bool(train)), i, 0)
+            if n_dim <= 8:
+                self._n_low_tiles += n_tiles
             for k in range(n_tiles):
-                tile_item.append(i)
+                tile_item.append(pos)
                 tile_start.append(k * self.tile_events)
                 tile_count.append(min(self.tile_events, n_events - k * self.tile_events))
                 tile_row.append(roff)
@@ -86,10 +94,11 @@ class VegasBatch:
             params.append(p)
             goff += n_dim * (BINS_MAX + 1)
             poff += p.size
-            blk_item.extend([i] * (n_dim + 1))
+            blk_item.extend([pos] * (n_dim + 1))
             blk_role.extend(list(range(n_dim)) + [-1])
-            self.dims.append(n_dim)
-            self.events.append(n_events)
+        for n_dim, n_events, integ in specs:
+            self.dims.append(int(n_dim))
+            self.events.append(int(n_events))
             self.integrands.append(integ)
         dev = self.device
         self.max_dim = max(self.dims)
@@ -97,7 +106,8 @@ class VegasBatch:
         self._items = torch.from_numpy(items.view(np.uint8).copy()).to(dev)
         self.grids = torch.as_tensor(np.concatenate(grids), dtype=torch.float64, device=dev)
         self.params = torch.as_tensor(np.concatenate(params), dtype=torch.float64, device=dev)
-        self._grid_off = items["grid_off"].copy()
+        self._grid_off = np.zeros(self.n_items, dtype=np.int64)
+        self._grid_off[items["slot"]] = items["grid_off"]  # by slot (the integral's index in specs)
         self._tile_item = torch.as_tensor(tile_item, dtype=torch.int32, device=dev)
         self._tile_start = torch.as_tensor(tile_start, dtype=torch.int64, device=dev)
         self._tile_count = torch.as_tensor(tile_count, dtype=torch.int32, device=dev)
@@ -109,11 +119,17 @@ class VegasBatch:
         self.avg = torch.zeros((self.n_items, 5), dtype=torch.float64, device=dev)
         self._calls = torch.zeros(self.n_items, dtype=torch.int32, device=dev)
         self._iters = torch.zeros(self.n_items, dtype=torch.int32, device=dev)
-        self._queue = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._queue = torch.zeros(2, dtype=torch.int32, device=dev)  # one work counter per class
         self._flags = torch.zeros(1, dtype=torch.int32, device=dev)
-        blocks, smem = ctypes.c_int(0), ctypes.c_int(0)
-        nat.check(nat.load().vf_batch_blocks(self.max_dim, ctypes.byref(blocks), ctypes.byref(smem)))
-        self.blocks = blocks.value
+        self._max_dim_low = max([d for d in self.dims if d <= 8], default=0)
+        self._max_dim_high = max([d for d in self.dims if d > 8], default=0)
+        self._blocks = {}
+        for md in (self._max_dim_low, self._max_dim_high):
+            if md:
+                blocks, smem = ctypes.c_int(0), ctypes.c_int(0)
+                nat.check(nat.load().vf_batch_blocks(md, ctypes.byref(blocks), ctypes.byref(smem)))
+                self._blocks[md] = blocks.value
+        self.blocks = max(self._blocks.values())
         self.iterations_done = 0
         self._graph = None
 
@@ -121,17 +137,23 @@ class VegasBatch:
     def _launch_iteration(self):
         lib = nat.load()
         s = nat.stream_handle()
-        nat.check(lib.vf_batch_sample(nat.ptr(self._items), nat.ptr(self._tile_item), nat.ptr(self._tile_start),
-                                      nat.ptr(self._tile_count), nat.ptr(self._tile_row), self.n_tiles,
-                                      self.max_dim, nat.ptr(self._queue), nat.ptr(self._calls),
-                                      nat.ptr(self.grids), nat.ptr(self.params), nat.ptr(self.partials),
-                                      self.seed, nat.ptr(self._flags), self.blocks, s))
+        lo = self._n_low_tiles
+        for first, count, md, q in ((0, lo, self._max_dim_low, 0), (lo, self.n_tiles - lo, self._max_dim_high, 1)):
+            if count == 0:
+                continue
+            nat.check(lib.vf_batch_sample(nat.ptr(self._items), nat.ptr(self._tile_item[first:]),
+                                          nat.ptr(self._tile_start[first:]), nat.ptr(self._tile_count[first:]),
+                                          nat.ptr(self._tile_row[first:]), count, md, nat.ptr(self._queue[q:q + 1]),
+                                          nat.ptr(self._calls), nat.ptr(self.grids), nat.ptr(self.params),
+                                          nat.ptr(self.partials), self.seed, nat.ptr(self._flags),
+                                          self._blocks[md], s))
         nat.check(lib.vf_batch_iteration_end(nat.ptr(self._items), nat.ptr(self._blk_item),
                                              nat.ptr(self._blk_role), int(self._blk_item.numel()),
                                              nat.ptr(self._tile_row), nat.ptr(self.partials),
                                              nat.ptr(self.grids), nat.ptr(self.history), nat.ptr(self.avg),
                                              self.hist_cap, nat.ptr(self._iters), nat.ptr(self._calls),
                                              nat.ptr(self._queue), nat.ptr(self._flags), s))
+        self._queue[1:2].zero_()  # the iteration end re-arms the first counter
 
     def reset_average(self):
         """Start a new weighted average (history slots restart at 0); the grids

@@ -24,14 +24,20 @@ int launched(const char* what) {
   return VF_OK;
 }
 
-// Raise the sampler's dynamic shared-memory limit once per size (a no-op
+// The sampler of a dimension class (n_dim <= 8, or any).
+const void* sample_kernel_for(int max_dim) {
+  return max_dim <= 8 ? (const void*)vf::vf_batch_sample_kernel<8> : (const void*)vf::vf_batch_sample_kernel<16>;
+}
+
+// Raise a sampler's dynamic shared-memory limit once per size (a no-op
 // afterwards, so launches inside a stream capture make no attribute calls).
-std::atomic<int> g_smem_set{0};
-cudaError_t set_smem(int smem) {
-  if (smem <= g_smem_set.load()) return cudaSuccess;
+std::atomic<int> g_smem_set[2] = {{0}, {0}};
+cudaError_t set_smem(int max_dim, int smem) {
+  std::atomic<int>& done = g_smem_set[max_dim <= 8 ? 0 : 1];
+  if (smem <= done.load()) return cudaSuccess;
   const cudaError_t e =
-      cudaFuncSetAttribute(vf::vf_batch_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess) g_smem_set.store(smem);
+      cudaFuncSetAttribute(sample_kernel_for(max_dim), cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) done.store(smem);
   return e;
 }
 
@@ -42,16 +48,13 @@ extern "C" {
 int vf_batch_blocks(int max_dim, int* blocks, int* smem_bytes) {
   if (!blocks || max_dim < 1 || max_dim > VF_MAX_DIM) return err(VF_ERR_ARG, "vf_batch_blocks: max_dim");
   const int smem = vf::batch_smem_bytes(max_dim);
-  cudaError_t e = set_smem(smem);
+  cudaError_t e = set_smem(max_dim, smem);
   if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
   // load the batch kernels now, so that a later stream capture launches only
-  cudaFuncAttributes attr;
-  if (cudaFuncGetAttributes(&attr, vf::vf_batch_end_kernel) != cudaSuccess ||
-      cudaFuncGetAttributes(&attr, vf::vf_batch_sample_kernel) != cudaSuccess)
+  if (vf::preload_batch_kernels() != cudaSuccess)
     return err(VF_ERR_CUDA, "vf_batch_blocks: loading the batch kernels failed");
-  (void)attr;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vf::vf_batch_sample_kernel, VF_THREADS, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sample_kernel_for(max_dim), VF_THREADS, smem);
   if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -91,9 +94,11 @@ int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long
     k1 += 0xBB67AE85u;
   }
   const int smem = vf::batch_smem_bytes(max_dim);
-  const cudaError_t e = set_smem(smem);
+  cudaError_t e = set_smem(max_dim, smem);
   if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
-  vf::vf_batch_sample_kernel<<<blocks, VF_THREADS, smem, (cudaStream_t)stream>>>(a);
+  void* args[] = {&a};
+  e = cudaLaunchKernel(sample_kernel_for(max_dim), dim3(blocks), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
+  if (e != cudaSuccess) return err(VF_ERR_LAUNCH, cudaGetErrorString(e));
   return launched("vf_batch_sample");
 }
 
@@ -129,7 +134,8 @@ int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, cons
 namespace vf {
 cudaError_t preload_batch_kernels() {
   cudaFuncAttributes attr;
-  cudaError_t e = cudaFuncGetAttributes(&attr, vf_batch_sample_kernel);
+  cudaError_t e = cudaFuncGetAttributes(&attr, vf_batch_sample_kernel<8>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_batch_sample_kernel<16>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_batch_end_kernel);
   return e;
 }

@@ -155,12 +155,15 @@ class VegasServer:
         self.avg = torch.zeros((self.max_slots, 5), dtype=torch.float64, device=dev)
         self.iters = torch.zeros(self.max_slots, dtype=torch.int32, device=dev)
         self.calls = torch.zeros(self.max_slots, dtype=torch.int32, device=dev)
-        self._queue = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._queue = torch.zeros(2, dtype=torch.int32, device=dev)  # one work counter per dimension class
         self._flags = torch.zeros(1, dtype=torch.int32, device=dev)
         self.partials = torch.zeros(1 << 20, dtype=torch.float64, device=dev)
-        blocks, smem = ctypes.c_int(0), ctypes.c_int(0)
-        nat.check(nat.load().vf_batch_blocks(MAX_DIM, ctypes.byref(blocks), ctypes.byref(smem)))
-        self.blocks = blocks.value
+        self._blocks = {}
+        for md in (8, MAX_DIM):  # the samplers of the two dimension classes
+            blocks, smem = ctypes.c_int(0), ctypes.c_int(0)
+            nat.check(nat.load().vf_batch_blocks(md, ctypes.byref(blocks), ctypes.byref(smem)))
+            self._blocks[md] = blocks.value
+        self.blocks = self._blocks[MAX_DIM]
         self._uniform_row = torch.as_tensor(np.linspace(0.0, 1.0, BINS_MAX + 1), dtype=torch.float64, device=dev)
         self.free_slots = list(range(self.max_slots - 1, -1, -1))
         self.active = []          # requests on the GPU
@@ -301,7 +304,8 @@ class VegasServer:
 
     def step(self, now_fn):
         """Advance every active request by one iteration, then retire finished ones."""
-        act = list(self.active)
+        # n_dim <= 8 first: those tiles go to the sampler of that dimension class
+        act = sorted(self.active, key=lambda r: r.n_dim > 8)
         t = self._tables(act)
         if t["rows_total"] > self.partials.numel():
             try:
@@ -323,17 +327,27 @@ class VegasServer:
                 for k in ("tile_item", "tile_start", "tile_count", "tile_row", "blk_item", "blk_role")}
         lib = nat.load()
         s = nat.stream_handle()
-        max_dim = int(max(r.n_dim for r in act))
-        nat.check(lib.vf_batch_sample(nat.ptr(items), nat.ptr(arrs["tile_item"]), nat.ptr(arrs["tile_start"]),
-                                      nat.ptr(arrs["tile_count"]), nat.ptr(arrs["tile_row"]), t["n_tiles"],
-                                      max_dim, nat.ptr(self._queue), nat.ptr(self.calls), nat.ptr(self.grids),
-                                      nat.ptr(self.params), nat.ptr(self.partials), self.seed,
-                                      nat.ptr(self._flags), self.blocks, s))
+        low = np.array([r.n_dim <= 8 for r in act])
+        n_low = int(t["items"]["n_tiles"][low].sum())
+        n_high = t["n_tiles"] - n_low
+        if n_low and n_high and min(n_low, n_high) < self._blocks[MAX_DIM]:
+            n_low = 0  # a small step: one launch of the general sampler over every tile
+        for first, count, md, q in ((0, n_low, 8, 0), (n_low, t["n_tiles"] - n_low, MAX_DIM, 1)):
+            if count == 0:
+                continue
+            nat.check(lib.vf_batch_sample(nat.ptr(items), nat.ptr(arrs["tile_item"][first:]),
+                                          nat.ptr(arrs["tile_start"][first:]), nat.ptr(arrs["tile_count"][first:]),
+                                          nat.ptr(arrs["tile_row"][first:]), count, md,
+                                          nat.ptr(self._queue[q:q + 1]), nat.ptr(self.calls), nat.ptr(self.grids),
+                                          nat.ptr(self.params), nat.ptr(self.partials), self.seed,
+                                          nat.ptr(self._flags), self._blocks[md], s))
         nat.check(lib.vf_batch_iteration_end(nat.ptr(items), nat.ptr(arrs["blk_item"]), nat.ptr(arrs["blk_role"]),
                                              int(t["blk_item"].size), nat.ptr(arrs["tile_row"]),
                                              nat.ptr(self.partials), nat.ptr(self.grids), nat.ptr(self.history),
                                              nat.ptr(self.avg), self.hist_cap, nat.ptr(self.iters),
                                              nat.ptr(self.calls), nat.ptr(self._queue), nat.ptr(self._flags), s))
+        if t["n_tiles"] - n_low:
+            self._queue[1:2].zero_()  # the second sampler's counter (the iteration end re-arms the first)
         slots = torch.as_tensor([r.slot for r in act], dtype=torch.int64, device=dev)
         state = torch.cat([self.avg[slots][:, 2:4].reshape(-1),
                            self.iters[slots].to(torch.float64)]).cpu().numpy()
