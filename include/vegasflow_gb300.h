@@ -46,6 +46,7 @@ extern "C" {
 /* ---- algorithms / precisions ---------------------------------------------- */
 #define VF_ALG_VEGAS 0  /* importance sampling, vflow.py:215                     */
 #define VF_ALG_PLAIN 1  /* plain MC, plain.py:11                                 */
+#define VF_ALG_PLUS 2   /* VEGAS+ samplers (vf_jit_integrand only), vflowplus.py:83 */
 #define VF_PREC_F64 0   /* the reference's float64 arithmetic                    */
 #define VF_PREC_F32 1   /* fused fp32 form, compensated sums, float64 across blocks */
 

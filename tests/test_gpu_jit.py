@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from vegasflow_gb300 import PlainFlow, VegasFlow, integrands
+from vegasflow_gb300 import PlainFlow, VegasFlow, VegasFlowPlus, integrands
 
 pytestmark = pytest.mark.gpu
 
@@ -35,7 +35,8 @@ def camel_exact(d):
     return one(P[0]) ** d + one(P[1]) ** d
 
 
-@pytest.mark.parametrize("cls,precision", [(VegasFlow, "fp32"), (VegasFlow, "fp64"), (PlainFlow, "fp32")])
+@pytest.mark.parametrize("cls,precision", [(VegasFlow, "fp32"), (VegasFlow, "fp64"), (PlainFlow, "fp32"),
+                                           (VegasFlowPlus, "fp32"), (VegasFlowPlus, "fp64")])
 def test_camel_against_exact(cls, precision):
     d = 4
     inst = cls(d, 1_000_000, verbose=False, precision=precision, seed=3)
@@ -72,3 +73,26 @@ def test_jit_error_is_reported():
     inst = VegasFlow(2, 1000, verbose=False)
     with pytest.raises(RuntimeError, match="NVRTC"):
         inst.compile(bad)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_plus_cuda_integrand_matches_builtin(precision):
+    """The same Gaussian as a CUDA-source integrand and as the built-in one in
+    VEGAS+ (adaptive): same estimate within the two sigmas."""
+    src = """
+__device__ vf_real g(const vf_real* x, int n_dim, vf_real weight, const double* p) {
+  vf_real s = 0;
+  for (int d = 0; d < n_dim; ++d) { vf_real t = (x[d] - (vf_real)0.5) / (vf_real)p[0]; s += t * t; }
+  return (vf_real)p[1] * exp(-s);
+}
+"""
+    a = 0.2
+    pref = (1.0 / a / math.sqrt(math.pi)) ** 3
+    out = []
+    for f in (integrands.cuda_integrand(src, "g", params=[a, pref]), integrands.symgauss(a)):
+        inst = VegasFlowPlus(3, 400_000, adaptive=True, verbose=False, precision=precision, seed=12)
+        inst.compile(f)
+        out.append(inst.run_integration(4))
+    (r1, s1), (r2, s2) = out
+    assert abs(r1 - r2) < 5 * math.hypot(s1, s2), out
+    assert abs(r1 - math.erf(0.5 / a) ** 3) < 5 * s1

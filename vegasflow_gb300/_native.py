@@ -31,6 +31,7 @@ VF_FLAG_HISTORY_FULL = 16
 
 VF_ALG_VEGAS = 0
 VF_ALG_PLAIN = 1
+VF_ALG_PLUS = 2
 VF_PREC_F64 = 0
 VF_PREC_F32 = 1
 

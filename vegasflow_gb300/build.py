@@ -67,7 +67,8 @@ def _compile(src, obj, verbose, extra):
     return obj
 
 
-JIT_HEADERS = ("vf_device.cuh", "vf_sample.cuh", "vf_vegas_f32.cuh")
+JIT_HEADERS = ("vf_device.cuh", "vf_sample.cuh", "vf_vegas_f32.cuh", "vf_plus_args.cuh", "vf_plus_sampler.cuh",
+               "vf_plus_f32.cuh")
 
 
 def write_jit_sources():

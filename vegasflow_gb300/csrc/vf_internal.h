@@ -42,6 +42,11 @@ cudaError_t preload_plus_kernels();
 cudaError_t preload_batch_kernels();
 cudaError_t preload_probe_kernels();
 
+// Launches the NVRTC-compiled VEGAS+ sampler of a JIT integrand with `args` (a
+// PlusArgs): the float32 one when `use_fast` and it exists, else the generic one.
+int jit_launch_plus(int integrand_id, int precision, int n_dim, void* args, int rows, int train, bool use_fast,
+                    void* stream);
+
 // Records an error message for vf_last_error_string(); returns `code`.
 int set_error(int code, const char* message);
 

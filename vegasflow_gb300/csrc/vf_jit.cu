@@ -19,6 +19,8 @@
 #include "vegasflow_gb300.h"
 #include "vf_internal.h"
 #include "vf_jit_sources.h"
+#include "vf_plus_f32.cuh"
+#include "vf_plus_sampler.cuh"
 #include "vf_vegas_f32.cuh"
 
 namespace {
@@ -58,44 +60,60 @@ const Driver& driver() {
 
 struct JitKernel {
   CUmodule module = nullptr;
-  CUfunction fn = nullptr;
-  int alg = 0, precision = 0, n_dim = 0, fast = 0, smem_set = 0;
+  CUfunction fn = nullptr;       // the sampler (VEGAS+: the float64 / tap-writing one)
+  CUfunction fn_fast = nullptr;  // VEGAS+ in fp32: the float32 sampler for Philox uniforms
+  int alg = 0, precision = 0, n_dim = 0, fast = 0, smem_set = 0, smem_set_fast = 0;
 };
 
 std::mutex g_mu;
 std::vector<JitKernel> g_kernels;
 
+// The program around a user integrand and the kernels to take from it: for
+// VEGAS and plain MC one sampler; for VEGAS+ the generic sampler and, in fp32,
+// also the float32 one.
 std::string program_text(const char* source, const char* func_name, int alg, int precision, int n_dim,
-                         std::string* expr) {
+                         std::vector<std::string>* exprs) {
   const bool fast = precision == VF_PREC_F32 && alg == VF_ALG_VEGAS;
+  const char* real = precision == VF_PREC_F64 ? "double" : "float";
   std::string src = "#define VF_JIT_USER 1\n";
-  src += std::string("typedef ") + (precision == VF_PREC_F64 ? "double" : "float") + " vf_real;\n";
+  src += std::string("typedef ") + real + " vf_real;\n";
   src += source;
   src += "\n#define VF_USER_FN " + std::string(func_name) + "\n";
-  src += fast ? "#include \"vf_vegas_f32.cuh\"\n" : "#include \"vf_sample.cuh\"\n";
-  if (fast) {
-    *expr = "vf::vf_vegas_f32_kernel<" + std::to_string(n_dim) + ", 99>";
+  exprs->clear();
+  if (alg == VF_ALG_PLUS) {
+    src += "#include \"vf_plus_sampler.cuh\"\n";
+    exprs->push_back(std::string("vf::vf_plus_kernel<") + real + ", " + std::to_string(vf::dim_bucket(n_dim)) +
+                     ", 99>");
+    if (precision == VF_PREC_F32) {
+      src += "#include \"vf_plus_f32.cuh\"\n";
+      exprs->push_back("vf::vf_plus_f32_kernel<" + std::to_string(n_dim) + ", 99>");
+    }
+  } else if (fast) {
+    src += "#include \"vf_vegas_f32.cuh\"\n";
+    exprs->push_back("vf::vf_vegas_f32_kernel<" + std::to_string(n_dim) + ", 99>");
   } else {
-    *expr = std::string("vf::vf_sample_kernel<") + (precision == VF_PREC_F64 ? "double" : "float") + ", " +
-            std::to_string(vf::dim_bucket(n_dim)) + ", 99>";
+    src += "#include \"vf_sample.cuh\"\n";
+    exprs->push_back(std::string("vf::vf_sample_kernel<") + real + ", " + std::to_string(vf::dim_bucket(n_dim)) +
+                     ", 99>");
   }
   return src;
 }
 
-// Compile; on success returns the CUBIN and the lowered kernel name.
+// Compile; on success returns the CUBIN and the lowered kernel names.
 int compile(const char* source, const char* func_name, int alg, int precision, int n_dim, std::vector<char>* cubin,
-            std::string* lowered, std::string* log) {
+            std::vector<std::string>* lowered, std::string* log) {
   if (!source || !func_name || !*func_name) return VF_ERR_ARG;
   if (n_dim < 1 || n_dim > VF_MAX_DIM) return VF_ERR_UNSUPPORTED;
-  if ((alg != VF_ALG_VEGAS && alg != VF_ALG_PLAIN) || (precision != VF_PREC_F64 && precision != VF_PREC_F32))
+  if ((alg != VF_ALG_VEGAS && alg != VF_ALG_PLAIN && alg != VF_ALG_PLUS) ||
+      (precision != VF_PREC_F64 && precision != VF_PREC_F32))
     return VF_ERR_ARG;
-  std::string expr;
-  const std::string src = program_text(source, func_name, alg, precision, n_dim, &expr);
+  std::vector<std::string> exprs;
+  const std::string src = program_text(source, func_name, alg, precision, n_dim, &exprs);
   nvrtcProgram prog;
   if (nvrtcCreateProgram(&prog, src.c_str(), "vf_user_integrand.cu", kJitHeaderCount, kJitHeaderSources,
                          kJitHeaderNames) != NVRTC_SUCCESS)
     return VF_ERR_JIT;
-  nvrtcAddNameExpression(prog, expr.c_str());
+  for (const std::string& e : exprs) nvrtcAddNameExpression(prog, e.c_str());
   const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
   const nvrtcResult rc = nvrtcCompileProgram(prog, 3, opts);
   size_t log_size = 0;
@@ -108,9 +126,14 @@ int compile(const char* source, const char* func_name, int alg, int precision, i
     nvrtcDestroyProgram(&prog);
     return VF_ERR_JIT;
   }
-  const char* name = nullptr;
-  nvrtcGetLoweredName(prog, expr.c_str(), &name);
-  if (lowered && name) *lowered = name;
+  if (lowered) {
+    lowered->clear();
+    for (const std::string& e : exprs) {
+      const char* name = nullptr;
+      nvrtcGetLoweredName(prog, e.c_str(), &name);
+      lowered->push_back(name ? name : "");
+    }
+  }
   if (cubin) {
     size_t n = 0;
     nvrtcGetCUBINSize(prog, &n);
@@ -124,6 +147,39 @@ int compile(const char* source, const char* func_name, int alg, int precision, i
 }  // namespace
 
 namespace vf {
+
+// Launch a VEGAS+ JIT kernel for vf_plus_sample (declared in vf_internal.h):
+// the float32 one when `use_fast` (fp32, Philox uniforms, no taps), else the
+// generic one.
+int jit_launch_plus(int integrand_id, int precision, int n_dim, void* args, int rows, int train, bool use_fast,
+                    void* stream) {
+  JitKernel k;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    const int idx = integrand_id - VF_INT_JIT_BASE;
+    if (idx < 0 || idx >= (int)g_kernels.size()) return set_error(VF_ERR_ARG, "unknown JIT integrand id");
+    k = g_kernels[idx];
+  }
+  if (k.alg != VF_ALG_PLUS || k.precision != precision || k.n_dim != n_dim)
+    return set_error(VF_ERR_ARG, "JIT integrand was compiled for another algorithm, precision or n_dim");
+  const bool fast = use_fast && k.fn_fast != nullptr;
+  const CUfunction fn = fast ? k.fn_fast : k.fn;
+  const int smem = fast ? plus_f32_smem_bytes(n_dim, train)
+                        : plus_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, train);
+  const Driver& drv = driver();
+  if (!drv.ok) return set_error(VF_ERR_CUDA, "CUDA driver entry points unavailable");
+  if (smem > 48 * 1024 && (fast ? k.smem_set_fast : k.smem_set) < smem) {
+    if (drv.func_set_attribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS)
+      return set_error(VF_ERR_CUDA, "cuFuncSetAttribute for a JIT kernel failed");
+    std::lock_guard<std::mutex> lock(g_mu);
+    JitKernel& kk = g_kernels[integrand_id - VF_INT_JIT_BASE];
+    (fast ? kk.smem_set_fast : kk.smem_set) = smem;
+  }
+  void* params[] = {args};
+  const CUresult r = drv.launch_kernel(fn, rows, 1, 1, VF_THREADS, 1, 1, smem, (CUstream)stream, params, nullptr);
+  if (r != CUDA_SUCCESS) return set_error(VF_ERR_LAUNCH, "cuLaunchKernel failed for a JIT kernel");
+  return VF_OK;
+}
 
 // Launch a JIT kernel for vf_sample (declared in vf_internal.h).
 int jit_launch(int integrand_id, int alg, int precision, int n_dim, void* args, int rows, int train, void* stream,
@@ -184,7 +240,8 @@ int vf_jit_integrand(const char* source, const char* func_name, int alg, int pre
                      int* integrand_id) {
   if (!integrand_id) return vf::set_error(VF_ERR_ARG, "vf_jit_integrand: integrand_id is NULL");
   std::vector<char> cubin;
-  std::string lowered, lg;
+  std::vector<std::string> lowered;
+  std::string lg;
   int rc = compile(source, func_name, alg, precision, n_dim, &cubin, &lowered, &lg);
   if (rc == VF_ERR_JIT) return vf::set_error(rc, ("NVRTC: " + lg).c_str());
   if (rc) return vf::set_error(rc, "vf_jit_integrand: bad arguments");
@@ -195,7 +252,9 @@ int vf_jit_integrand(const char* source, const char* func_name, int alg, int pre
   JitKernel k;
   if (drv.module_load_data(&k.module, cubin.data()) != CUDA_SUCCESS)
     return vf::set_error(VF_ERR_JIT, "vf_jit_integrand: cuModuleLoadData failed");
-  if (drv.module_get_function(&k.fn, k.module, lowered.c_str()) != CUDA_SUCCESS)
+  if (lowered.empty() || drv.module_get_function(&k.fn, k.module, lowered[0].c_str()) != CUDA_SUCCESS)
+    return vf::set_error(VF_ERR_JIT, "vf_jit_integrand: kernel not found in the module");
+  if (lowered.size() > 1 && drv.module_get_function(&k.fn_fast, k.module, lowered[1].c_str()) != CUDA_SUCCESS)
     return vf::set_error(VF_ERR_JIT, "vf_jit_integrand: kernel not found in the module");
   k.alg = alg;
   k.precision = precision;

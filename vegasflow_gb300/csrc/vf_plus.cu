@@ -83,7 +83,8 @@ int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, in
   if (!grid || !n_ev || !ev_start || n_strat < 1 || n_hcubes < 1 || rows < 1)
     return err(VF_ERR_ARG, "vf_plus_sample: NULL buffer or bad stratification");
   if ((xmin == nullptr) != (xdelta == nullptr)) return err(VF_ERR_ARG, "vf_plus_sample: xmin/xdelta");
-  if (integrand < VF_INT_NONE || integrand > VF_INT_SUM) return err(VF_ERR_ARG, "vf_plus_sample: integrand");
+  const bool jit = integrand >= VF_INT_JIT_BASE;
+  if ((integrand < VF_INT_NONE || integrand > VF_INT_SUM) && !jit) return err(VF_ERR_ARG, "vf_plus_sample: integrand");
   if (integrand != VF_INT_NONE && (!ress || !ress2 || !partials))
     return err(VF_ERR_ARG, "vf_plus_sample: ress/ress2/partials required when evaluating");
   if ((integrand == VF_INT_SYMGAUSS || integrand == VF_INT_GAUSS || integrand == VF_INT_BREIT_WIGNER) && !params)
@@ -91,8 +92,8 @@ int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, in
   // fp32 with a built-in integrand and Philox uniforms: the float32 kernel
   const bool f32 = precision == VF_PREC_F32 && integrand >= VF_INT_SYMGAUSS && integrand <= VF_INT_SUM &&
                    !u_inj && !ind_out && !x_out && !w_out;
-  const void* k = f32 ? vf::plus_f32_kernel(n_dim, integrand) : plus_kernel(precision, n_dim, integrand);
-  if (!k) return err(VF_ERR_UNSUPPORTED, "vf_plus_sample: no kernel");
+  const void* k = jit ? nullptr : (f32 ? vf::plus_f32_kernel(n_dim, integrand) : plus_kernel(precision, n_dim, integrand));
+  if (!k && !jit) return err(VF_ERR_UNSUPPORTED, "vf_plus_sample: no kernel");
   vf::PlusArgs a;
   a.grid = grid;
   a.n_ev = n_ev;
@@ -123,6 +124,11 @@ int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, in
   }
   for (int q = 0; q < 8; ++q) a.ctr2[q] = (call_ctr << 4) | (unsigned int)q;
   a.ctr3 = call_ctr >> 28;
+  if (jit) {
+    const bool fast = precision == VF_PREC_F32 && !u_inj && !ind_out && !x_out && !w_out;
+    const int rc = vf::jit_launch_plus(integrand, precision, n_dim, &a, rows, a.train, fast, stream);
+    return rc ? rc : launched("vf_plus_sample (JIT)");
+  }
   const int smem = f32 ? vf::plus_f32_smem_bytes(n_dim, a.train)
                        : vf::plus_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, a.train);
   void* args[] = {&a};

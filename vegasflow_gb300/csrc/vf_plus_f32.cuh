@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(VF_THREADS) vf_plus_f32_kernel(const PlusArgs 
   __syncthreads();
   const float wscale = s_wscale;
   IntegrandConsts<float, D> kc;
-  load_consts<D>(kc, INTEG, a.params, D);
+  load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
   float* my_hist = hist + warp * NB;
   const u32 ns = (u32)a.n_strat;
   const float inv_ns = 1.0f / (float)ns;
@@ -105,7 +105,13 @@ __global__ void __launch_bounds__(VF_THREADS) vf_plus_f32_kernel(const PlusArgs 
           }
         }
       }
-      const float f = eval_builtin<D>(INTEG, x, D, kc);
+      float f;
+#ifdef VF_JIT_USER
+      if constexpr (INTEG == VF_INT_USER)
+        f = (float)VF_USER_FN(x, D, wf * wh, a.params);
+      else
+#endif
+        f = eval_builtin<D>(INTEG, x, D, kc);
       const float v = wf * wh * f;  // vflowplus.py:209
       const float v2 = v * v;
       two_sum_add(s1, v);

@@ -145,8 +145,8 @@ class VegasFlowPlus(VegasFlow):
         self._n_ev_stale = True
 
     def _compile_cuda_integrand(self, integrand):
-        raise NotImplementedError("VegasFlowPlus evaluates built-in device integrands and torch callables; "
-                                  "CUDA-source integrands run with VegasFlow and PlainFlow")
+        """NVRTC-compile the user's device function into the VEGAS+ samplers."""
+        return integrand.compile_for(nat.VF_ALG_PLUS, self._prec, self.n_dim)
 
     def _plus_rows(self):
         import ctypes
