@@ -20,6 +20,31 @@ namespace vf {
 // events per thread per tile
 #define VF_MAP_EPT 2
 
+// resident blocks per SM the register allocation is sized for (256 threads)
+#ifndef VF_MAP_MIN_BLOCKS
+#define VF_MAP_MIN_BLOCKS VF_F32_MIN_BLOCKS
+#endif
+
+// One event's row of D 32-bit words into the staging tile in 16-byte stores (D a
+// multiple of 4), 8-byte stores (D even) or word stores (D odd: conflict-free).
+// Rows are 4 D bytes apart, so a warp storing word by word puts gcd(D, 32) lanes
+// on one bank (8 at D = 8); a 16-byte store is served per quarter-warp, whose 8
+// lanes then share a bank at most D / 4 ways (2 at D = 8).
+template <int D>
+__device__ __forceinline__ void stage_row(u32* dst, const u32 (&v)[D]) {
+  if constexpr (D % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < D / 4; ++q)
+      reinterpret_cast<uint4*>(dst)[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  } else if constexpr (D % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < D / 2; ++q) reinterpret_cast<uint2*>(dst)[q] = make_uint2(v[2 * q], v[2 * q + 1]);
+  } else {
+#pragma unroll
+    for (int d = 0; d < D; ++d) dst[d] = v[d];
+  }
+}
+
 __host__ __device__ inline int vegas_f32_map_smem_bytes(int D, int threads, bool with_ind) {
   const int stage = VF_MAP_EPT * threads * (D * 4 * (with_ind ? 2 : 1) + 4);
   return D * VF_BINS * 8 + 2 * stage + 128;
@@ -31,7 +56,7 @@ __device__ __forceinline__ void bulk_store(void* gdst, u32 ssrc, u32 bytes) {
 }
 
 template <int D, int THREADS = VF_THREADS>
-__global__ void __launch_bounds__(THREADS, VF_F32_MIN_BLOCKS * VF_THREADS / THREADS)
+__global__ void __launch_bounds__(THREADS, VF_MAP_MIN_BLOCKS * VF_THREADS / THREADS)
 vf_vegas_f32_map_kernel(const __grid_constant__ SampleArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NB = D * VF_BINS;
@@ -81,8 +106,8 @@ vf_vegas_f32_map_kernel(const __grid_constant__ SampleArgs a) {
     const long long e0 = t * T;
     const bool full = aligned && e0 + T <= n;
     unsigned char* st = stage0 + (it & 1) * stage_bytes;
-    float* xs = reinterpret_cast<float*>(st);
-    int* is = reinterpret_cast<int*>(st + XB);
+    u32* xs = reinterpret_cast<u32*>(st);
+    u32* is = reinterpret_cast<u32*>(st + XB);
     float* wsm = reinterpret_cast<float*>(st + XB * (want_ind ? 2 : 1));
     if (full) {
       // the stage's previous tile (two tiles back) must have been read out
@@ -96,8 +121,8 @@ vf_vegas_f32_map_kernel(const __grid_constant__ SampleArgs a) {
       if (e < n) {
         const u64 ev = (u64)(a.ev_offset + e);
         float wf = 1.0f;
-        float xr[D];
-        int br[D];
+        u32 xr[D];  // x as float bits
+        u32 br[D];
 #pragma unroll
         for (int q = 0; q < (D + 3) / 4; ++q) {
           u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = cw.c2base | (u32)q, c3 = cw.c3;
@@ -111,27 +136,24 @@ vf_vegas_f32_map_kernel(const __grid_constant__ SampleArgs a) {
               const int i = (int)(pp >> 32);
               const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
               const float2 c = cells[d * VF_BINS + i];
-              xr[d] = fmaf(c.y, m, c.x);
+              xr[d] = __float_as_uint(fmaf(c.y, m, c.x));
               wf = (d == 0) ? c.y : wf * c.y;
-              br[d] = i;
+              br[d] = (u32)i;
             }
           }
         }
         const float w = wf * wscale;
         if (full) {
-#pragma unroll
-          for (int d = 0; d < D; ++d) xs[r * D + d] = xr[d];
-          if (want_ind)
-#pragma unroll
-            for (int d = 0; d < D; ++d) is[r * D + d] = br[d];
+          stage_row<D>(xs + r * D, xr);
+          if (want_ind) stage_row<D>(is + r * D, br);
           wsm[r] = w;
         } else {
           if (x_out)
 #pragma unroll
-            for (int d = 0; d < D; ++d) x_out[e * D + d] = xr[d];
+            for (int d = 0; d < D; ++d) x_out[e * D + d] = __uint_as_float(xr[d]);
           if (want_ind)
 #pragma unroll
-            for (int d = 0; d < D; ++d) ind_out[e * D + d] = br[d];
+            for (int d = 0; d < D; ++d) ind_out[e * D + d] = (int)br[d];
           if (w_out) w_out[e] = w;
         }
       }
