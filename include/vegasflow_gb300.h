@@ -47,6 +47,7 @@ extern "C" {
 #define VF_ALG_VEGAS 0  /* importance sampling, vflow.py:215                     */
 #define VF_ALG_PLAIN 1  /* plain MC, plain.py:11                                 */
 #define VF_ALG_PLUS 2   /* VEGAS+ samplers (vf_jit_integrand only), vflowplus.py:83 */
+#define VF_ALG_BATCH 3  /* batched sampler (vf_jit_integrand only): vf_batch_sample_jit */
 #define VF_PREC_F64 0   /* the reference's float64 arithmetic                    */
 #define VF_PREC_F32 1   /* fused fp32 form, compensated sums, float64 across blocks */
 
@@ -220,7 +221,7 @@ typedef struct vf_batch_item {
   long long param_off;  /* doubles into params */
   double xjac;          /* 1 / n_events */
   int n_dim;
-  int integrand;        /* VF_INT_SYMGAUSS .. VF_INT_SUM */
+  int integrand;        /* VF_INT_SYMGAUSS .. VF_INT_SUM (vf_batch_sample), or the id of vf_batch_sample_jit */
   int stream_id;
   int tile0;            /* first tile of this integral */
   int n_tiles;
@@ -236,6 +237,13 @@ int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long
                     const int* tile_count, const long long* tile_row, int n_tiles, int max_dim, int* queue,
                     const unsigned int* calls, const double* grids, const double* params, double* partials,
                     unsigned long long seed, int* flags, int blocks, void* stream);
+/* vf_batch_sample with a user integrand: every integral of the tiles given uses
+ * integrand_id (vf_jit_integrand with VF_ALG_BATCH, VF_PREC_F32 and n_dim >= max_dim),
+ * its parameters at params + param_off. */
+int vf_batch_sample_jit(int integrand_id, const vf_batch_item* items, const int* tile_item,
+                        const long long* tile_start, const int* tile_count, const long long* tile_row, int n_tiles,
+                        int max_dim, int* queue, const unsigned int* calls, const double* grids, const double* params,
+                        double* partials, unsigned long long seed, int* flags, int blocks, void* stream);
 /* Per integral: sums of its tile rows in tile order, sigma, history[slot][iters[slot]],
  * the weighted average avg[slot][5], then iters[slot] += 1, calls[slot] += 1; per
  * (integral, dimension) block: refinement of that grid row; *queue = 0.  Block b serves
@@ -284,7 +292,10 @@ int vf_vegas_iteration_static(int precision, double* grid, int n_dim, long long 
  * vf_sample `params` pointer.  NVRTC compiles it with the sampler into a kernel
  * for (alg, precision, n_dim) -- the fp32 VEGAS kernel specialised on n_dim, or
  * the generic sampler -- built for sm_103a and loaded into the current context;
- * *integrand_id (>= VF_INT_JIT_BASE) then selects it in vf_sample.  This call
+ * *integrand_id (>= VF_INT_JIT_BASE) then selects it in vf_sample (VF_ALG_VEGAS,
+ * VF_ALG_PLAIN), vf_plus_sample (VF_ALG_PLUS) or vf_batch_sample_jit
+ * (VF_ALG_BATCH, fp32 only: the batched sampler for integrals of up to n_dim
+ * dimensions, the function called with each integral's own n_dim).  This call
  * compiles on the host and loads a module: it is not for hot paths.
  */
 int vf_jit_integrand(const char* source, const char* func_name, int alg, int precision, int n_dim,

@@ -173,9 +173,11 @@ __device__ vf_real camel(const vf_real* x, int n_dim, vf_real weight, const doub
 def test_cuda_integrand_compiles_without_gpu():
     """NVRTC compiles the user source with the sampler on the host."""
     f = integrands.cuda_integrand(CAMEL_SRC, "camel", params=[0.3, 0.7, 0.1])
-    for alg, prec in ((0, 1), (0, 0), (1, 1), (1, 0), (2, 1), (2, 0)):
+    for alg, prec in ((0, 1), (0, 0), (1, 1), (1, 0), (2, 1), (2, 0), (3, 1)):
         ok, log = f.check(alg, prec, 5)
         assert ok, log
+    ok, _ = f.check(3, 0, 5)  # the batched sampler is fp32 only
+    assert not ok
     bad = integrands.cuda_integrand("__device__ vf_real bad(const vf_real* x) { return y; }", "bad")
     ok, log = bad.check()
     assert not ok and "undefined" in log

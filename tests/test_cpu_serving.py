@@ -4,7 +4,7 @@ import numpy as np
 
 from vegasflow_gb300 import integrands
 from vegasflow_gb300.batch import ITEM_DTYPE, c4_specs
-from vegasflow_gb300.serving import percentile, poisson_workload, request_footprint, step_tables
+from vegasflow_gb300.serving import launch_groups, percentile, poisson_workload, request_footprint, step_tables
 
 
 def test_step_tables_cover_every_event():
@@ -53,3 +53,18 @@ def test_percentile_and_c4_specs():
     assert len(specs) == 1024
     assert all(2 <= d <= 16 and 10_000 <= n <= 10_000_000 for d, n, _ in specs)
     assert all(isinstance(f, integrands.DeviceIntegrand) for _, _, f in specs)
+
+
+def test_launch_groups():
+    """One sampler launch per run of (program, dimension class); the built-in
+    classes share one launch when either is smaller than the persistent grid."""
+    from types import SimpleNamespace as R
+
+    act = [R(program=0, n_dim=4), R(program=0, n_dim=6), R(program=0, n_dim=12), R(program=1001, n_dim=3),
+           R(program=1002, n_dim=9), R(program=1002, n_dim=16)]
+    tiles = [10, 5, 400, 7, 3, 2]
+    assert launch_groups(act, tiles, 10) == [(0, 15, 8, None), (15, 400, 16, None), (415, 7, 8, 1001),
+                                             (422, 5, 16, 1002)]
+    assert launch_groups(act, tiles, 100) == [(0, 415, 16, None), (415, 7, 8, 1001), (422, 5, 16, 1002)]
+    assert launch_groups(act[3:], tiles[3:], 100) == [(0, 7, 8, 1001), (7, 5, 16, 1002)]
+    assert launch_groups([], [], 100) == []

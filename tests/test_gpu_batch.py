@@ -1,6 +1,7 @@
 """Batched VEGAS (one persistent launch per iteration over many integrals):
-alone vs in the mix, CUDA-graph replay vs eager launches, and the 1,024-integral
-workload against the exact integrals."""
+alone vs in the mix, CUDA-graph replay vs eager launches, CUDA-source integrands
+beside the built-in ones, and the 1,024-integral workload against the exact
+integrals."""
 
 import math
 
@@ -78,6 +79,54 @@ def test_mixed_batch_against_exact():
     for i, (d, n, f) in enumerate(specs):
         ex = _exact(d, f)
         assert abs(mean[i] - ex) < 5 * sigma[i], (i, f.__name__, mean[i], sigma[i], ex)
+
+
+USER_GAUSS_SRC = r"""
+__device__ vf_real ugauss(const vf_real* x, int n_dim, vf_real weight, const double* p) {
+  // prod_d exp(-((x_d - mu) / a)^2) / (a sqrt(pi)),  mu = p[0], a = p[1]
+  const vf_real mu = (vf_real)p[0], a = (vf_real)p[1], norm = (vf_real)(0.5641895835477563 / p[1]);
+  vf_real s = 0, f = 1;
+  for (int d = 0; d < n_dim; ++d) {
+    const vf_real t = (x[d] - mu) / a;
+    s += t * t;
+    f *= norm;
+  }
+  return f * exp(-s);
+}
+"""
+
+
+def test_cuda_integrand_in_a_batch():
+    """A CUDA-source integrand in a batch: its integrals (several n_dim, both
+    dimension classes) run in launches of their own beside the built-in ones.
+    Each gives its exact integral, the same numbers alone as in the mix, and on
+    its first iteration the built-in integrand of the same function's estimate
+    (same seed and stream id: the same events)."""
+    user = integrands.cuda_integrand(USER_GAUSS_SRC, "ugauss", params=[0.5, 0.2])
+    specs = _mixed_specs()[:3] + [(4, 200_000, user), (10, 300_000, user), (2, 50_000, user)]
+    mix = VegasBatch(specs, seed=21)
+    assert sum(g[3] is not None for g in mix._groups) == 2  # one user launch per dimension class
+    mix.run(4)
+    mean, sigma, chi2, flags = mix.results()
+    assert flags == 0
+    for i, (d, n, f) in enumerate(specs):
+        ex = oracle.symgauss_exact(d, 0.2) if f is user else _exact(d, f)
+        assert abs(mean[i] - ex) < 5 * sigma[i], (i, mean[i], sigma[i], ex)
+    h_mix = mix.history_host()
+    for i in (3, 4):
+        alone = VegasBatch([specs[i]], seed=21, stream_ids=[i])
+        alone.run(4)
+        h = alone.history_host()[0]
+        np.testing.assert_allclose(h[0], h_mix[i, 0], rtol=1e-12)
+        np.testing.assert_allclose(h, h_mix[i], rtol=1e-5)
+    for i in (3, 4):
+        d, n, _ = specs[i]
+        ref = VegasBatch([(d, n, integrands.symgauss(0.2))], seed=21, stream_ids=[i])
+        ref.run(1)
+        np.testing.assert_allclose(h_mix[i, 0], ref.history_host()[0, 0], rtol=1e-4)
+    graphed = VegasBatch(specs, seed=21)
+    graphed.run(4, graph=True)
+    np.testing.assert_allclose(graphed.history_host()[:, 0], h_mix[:, 0], rtol=1e-12)
 
 
 def test_c4_1024_integrals():

@@ -64,6 +64,62 @@ def test_results_against_exact():
         assert abs(r.result - ex) < 5 * r.sigma
 
 
+USER_GAUSS_SRC = r"""
+__device__ vf_real ugauss(const vf_real* x, int n_dim, vf_real weight, const double* p) {
+  // prod_d exp(-((x_d - mu) / a)^2) / (a sqrt(pi)),  mu = p[0], a = p[1]
+  const vf_real mu = (vf_real)p[0], a = (vf_real)p[1], norm = (vf_real)(0.5641895835477563 / p[1]);
+  vf_real s = 0, f = 1;
+  for (int d = 0; d < n_dim; ++d) {
+    const vf_real t = (x[d] - mu) / a;
+    s += t * t;
+    f *= norm;
+  }
+  return f * exp(-s);
+}
+"""
+
+
+def test_cuda_source_requests():
+    """CUDA-source integrands as requests: compiled at submission, served by their
+    own sampler launches (one per dimension class) beside built-in requests that
+    arrive later; each result is within 5 sigma of the exact integral and the
+    same alone as in the mix."""
+    import math
+
+    user = integrands.cuda_integrand(USER_GAUSS_SRC, "ugauss", params=[0.5, 0.2])
+
+    def reqs():
+        r = _requests()[:3]
+        r += [Request(3, 100_000, user, target_rel_sigma=2e-3, max_iterations=10, rid=10),
+              Request(11, 300_000, user, target_rel_sigma=2e-3, max_iterations=10, rid=11)]
+        return r
+
+    mix_reqs = reqs()
+    server = VegasServer(max_slots=64, seed=41)
+    for r in mix_reqs[3:]:
+        assert server.submit(r)
+    assert mix_reqs[3].program != mix_reqs[4].program  # a sampler build per dimension class
+    server._admit(0.0)
+    server.step(lambda: 0.0)
+    for r in mix_reqs[:3]:
+        server.submit(r)
+    while server.waiting or server.active:
+        server._admit(0.0)
+        server.step(lambda: 0.0)
+    mix = {r.rid: r for r in server.done}
+    assert len(mix) == 5 and all(r.status in ("converged", "finished") for r in mix.values())
+    for rid in (10, 11):
+        r = mix[rid]
+        assert abs(r.result - math.erf(2.5) ** r.n_dim) < 5 * r.sigma, (rid, r.result, r.sigma)
+    for r in reqs()[3:]:
+        alone = VegasServer(max_slots=4, seed=41)
+        alone.run([r], realtime=False)
+        got = alone.done[0]
+        m = mix[r.rid]
+        assert got.iterations == m.iterations
+        np.testing.assert_allclose([got.result, got.sigma], [m.result, m.sigma], rtol=1e-5)
+
+
 def test_short_realtime_run():
     reqs = poisson_workload(rate=200.0, duration=2.0, seed=9)
     server = VegasServer(max_slots=2048, seed=1)
@@ -88,14 +144,15 @@ def test_rejections_do_not_stop_the_server():
     bad = [Request(17, 1000, integrands.symgauss(), rid=1),                                   # dimensions
            Request(2, 1, integrands.symgauss(), rid=2),                                       # events
            Request(4, 1000, integrands.cuda_integrand("__device__ vf_real f(const vf_real* x, int n, "
-                                                     "vf_real w, const double* p) { return x[0]; }",
-                                                     "f"), rid=3),                            # not built in
+                                                     "vf_real w, const double* p) { return y[0]; }",
+                                                     "f"), rid=3),                            # does not compile
            Request(3, 1000, integrands.gauss([0.5, 0.5], [0.1, 0.1]), rid=4),                 # params for 2-D
            Request(16, 10 ** 9, integrands.symgauss(), rid=5)]                               # over the budget
     assert server.submit(good)
     for r in bad:
         assert not server.submit(r)
         assert r.status == "rejected" and r.error
+    assert "did not compile" in bad[2].error
     _drive(server, 4)
     assert good.status == "finished" and good.iterations == 3
 

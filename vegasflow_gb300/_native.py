@@ -32,6 +32,7 @@ VF_FLAG_HISTORY_FULL = 16
 VF_ALG_VEGAS = 0
 VF_ALG_PLAIN = 1
 VF_ALG_PLUS = 2
+VF_ALG_BATCH = 3
 VF_PREC_F64 = 0
 VF_PREC_F32 = 1
 
@@ -78,6 +79,7 @@ SIGNATURES = {
                               _P, _I, _P, _P],
     "vf_batch_blocks": [_I, _P, _P],
     "vf_batch_sample": [_P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],
+    "vf_batch_sample_jit": [_I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],
     "vf_batch_iteration_end": [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P],
     "vf_jit_integrand": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, _P],
     "vf_jit_check": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, ctypes.c_char_p, _I],

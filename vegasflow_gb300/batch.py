@@ -23,7 +23,7 @@ import torch
 
 from . import _native as nat
 from .configflow import BINS_MAX
-from .integrands import DeviceIntegrand
+from .integrands import CudaIntegrand, DeviceIntegrand
 from .utils import preload_kernels
 
 ITEM_DTYPE = np.dtype([("n_events", "<i8"), ("grid_off", "<i8"), ("param_off", "<i8"), ("xjac", "<f8"),
@@ -38,7 +38,10 @@ class VegasBatch:
     """Integrate many integrals together.
 
     ``specs``: iterable of ``(n_dim, n_events, integrand)`` with ``integrand`` a
-    ``DeviceIntegrand`` (built-in; Gaussian family, Breit-Wigner, prod, sum).
+    built-in ``DeviceIntegrand`` (Gaussian family, Breit-Wigner, prod, sum) or a
+    ``CudaIntegrand`` (CUDA source; NVRTC builds a batched sampler around it,
+    and its integrals run in a launch of their own, each with its own n_dim and
+    the integrand's parameters).
     ``stream_ids``: optional per-integral Philox stream ids (default 0, 1, ...);
     an integral run with the same seed and stream id gives the same numbers in
     any batch."""
@@ -64,26 +67,46 @@ class VegasBatch:
         blk_item, blk_role = [], []
         goff = poff = roff = 0
         self.dims, self.events, self.integrands = [], [], []
-        # integrals with n_dim <= 8 first: their tiles go to the sampler of that
-        # dimension class (smaller shared tables, more blocks per SM); the slot
-        # (result index) stays the integral's position in `specs`
-        order = sorted(range(self.n_items), key=lambda i: int(specs[i][0]) > 8)
-        self._n_low_tiles = 0
+        # Launch groups: one sampler launch per (dimension class, program).  The
+        # class: integrals with n_dim <= 8 go to the sampler with smaller shared
+        # tables and more blocks per SM.  The program: the built-in integrands
+        # share one sampler; each CUDA-source integrand has its own.  Items are
+        # ordered by group so that each launch's tiles are contiguous; the slot
+        # (result index) stays the integral's position in `specs`.
+        user = []  # distinct CudaIntegrand objects, in order of appearance
+        for i, (n_dim, n_events, integ) in enumerate(specs):
+            if isinstance(integ, CudaIntegrand):
+                if not any(u is integ for u in user):
+                    user.append(integ)
+            elif not isinstance(integ, DeviceIntegrand) or not 1 <= integ.integrand_id <= nat.VF_INT_SUM:
+                raise TypeError("batched integrals need a built-in DeviceIntegrand or a CudaIntegrand")
+            if not 1 <= int(n_dim) <= 16 or int(n_events) < 2:
+                raise ValueError(f"integral {i}: n_dim={n_dim}, n_events={n_events}")
+
+        def group_of(i):
+            n_dim, _, integ = specs[i]
+            prog = next((k + 1 for k, u in enumerate(user) if u is integ), 0)
+            return (int(int(n_dim) > 8), prog)
+
+        order = sorted(range(self.n_items), key=group_of)
+        group_tiles = {}  # (class, program) -> [first tile, tiles, largest n_dim]
         for pos, i in enumerate(order):  # pos: the integral's place in the items array
             n_dim, n_events, integ = specs[i]
             n_dim, n_events = int(n_dim), int(n_events)
-            if not isinstance(integ, DeviceIntegrand) or not 1 <= integ.integrand_id <= nat.VF_INT_SUM:
-                raise TypeError("batched integrals need a built-in DeviceIntegrand")
-            if not 1 <= n_dim <= 16 or n_events < 2:
-                raise ValueError(f"integral {i}: n_dim={n_dim}, n_events={n_events}")
             integ.check_dims(n_dim)
             p = integ.params(n_dim)
+            g = group_of(i)
+            if g[1]:  # the id of the program's batched sampler for this class
+                integ_id = integ.compile_for(nat.VF_ALG_BATCH, nat.VF_PREC_F32, 16 if g[0] else 8)
+            else:
+                integ_id = integ.integrand_id
             n_tiles = (n_events + self.tile_events - 1) // self.tile_events
             width = 2 + BINS_MAX * n_dim
-            items[pos] = (n_events, goff, poff, 1.0 / n_events, n_dim, integ.integrand_id, stream_ids[i],
+            gt = group_tiles.setdefault(g, [len(tile_item), 0, 0])
+            gt[1] += n_tiles
+            gt[2] = max(gt[2], n_dim)
+            items[pos] = (n_events, goff, poff, 1.0 / n_events, n_dim, integ_id, stream_ids[i],
                           len(tile_item), n_tiles, int(bool(train)), i, 0)
-            if n_dim <= 8:
-                self._n_low_tiles += n_tiles
             for k in range(n_tiles):
                 tile_item.append(pos)
                 tile_start.append(k * self.tile_events)
@@ -119,16 +142,20 @@ class VegasBatch:
         self.avg = torch.zeros((self.n_items, 5), dtype=torch.float64, device=dev)
         self._calls = torch.zeros(self.n_items, dtype=torch.int32, device=dev)
         self._iters = torch.zeros(self.n_items, dtype=torch.int32, device=dev)
-        self._queue = torch.zeros(2, dtype=torch.int32, device=dev)  # one work counter per class
         self._flags = torch.zeros(1, dtype=torch.int32, device=dev)
-        self._max_dim_low = max([d for d in self.dims if d <= 8], default=0)
-        self._max_dim_high = max([d for d in self.dims if d > 8], default=0)
+        # launches: (first tile, tiles, largest n_dim, JIT id or None); the
+        # sampler's persistent grid follows the class's built-in kernel (a JIT
+        # build has the same launch bounds and shared memory)
+        self._groups = []
         self._blocks = {}
-        for md in (self._max_dim_low, self._max_dim_high):
-            if md:
+        for (cls, prog), (first, count, md) in sorted(group_tiles.items()):
+            jit = int(items[tile_item[first]]["integrand"]) if prog else None
+            self._groups.append((first, count, md, jit))
+            if md not in self._blocks:
                 blocks, smem = ctypes.c_int(0), ctypes.c_int(0)
                 nat.check(nat.load().vf_batch_blocks(md, ctypes.byref(blocks), ctypes.byref(smem)))
                 self._blocks[md] = blocks.value
+        self._queue = torch.zeros(len(self._groups), dtype=torch.int32, device=dev)  # a work counter per launch
         self.blocks = max(self._blocks.values())
         self.iterations_done = 0
         self._graph = None
@@ -137,23 +164,23 @@ class VegasBatch:
     def _launch_iteration(self):
         lib = nat.load()
         s = nat.stream_handle()
-        lo = self._n_low_tiles
-        for first, count, md, q in ((0, lo, self._max_dim_low, 0), (lo, self.n_tiles - lo, self._max_dim_high, 1)):
-            if count == 0:
-                continue
-            nat.check(lib.vf_batch_sample(nat.ptr(self._items), nat.ptr(self._tile_item[first:]),
-                                          nat.ptr(self._tile_start[first:]), nat.ptr(self._tile_count[first:]),
-                                          nat.ptr(self._tile_row[first:]), count, md, nat.ptr(self._queue[q:q + 1]),
-                                          nat.ptr(self._calls), nat.ptr(self.grids), nat.ptr(self.params),
-                                          nat.ptr(self.partials), self.seed, nat.ptr(self._flags),
-                                          self._blocks[md], s))
+        for q, (first, count, md, jit) in enumerate(self._groups):
+            args = (nat.ptr(self._items), nat.ptr(self._tile_item[first:]), nat.ptr(self._tile_start[first:]),
+                    nat.ptr(self._tile_count[first:]), nat.ptr(self._tile_row[first:]), count, md,
+                    nat.ptr(self._queue[q:q + 1]), nat.ptr(self._calls), nat.ptr(self.grids), nat.ptr(self.params),
+                    nat.ptr(self.partials), self.seed, nat.ptr(self._flags), self._blocks[md], s)
+            if jit is None:
+                nat.check(lib.vf_batch_sample(*args))
+            else:
+                nat.check(lib.vf_batch_sample_jit(jit, *args))
         nat.check(lib.vf_batch_iteration_end(nat.ptr(self._items), nat.ptr(self._blk_item),
                                              nat.ptr(self._blk_role), int(self._blk_item.numel()),
                                              nat.ptr(self._tile_row), nat.ptr(self.partials),
                                              nat.ptr(self.grids), nat.ptr(self.history), nat.ptr(self.avg),
                                              self.hist_cap, nat.ptr(self._iters), nat.ptr(self._calls),
                                              nat.ptr(self._queue), nat.ptr(self._flags), s))
-        self._queue[1:2].zero_()  # the iteration end re-arms the first counter
+        if len(self._groups) > 1:
+            self._queue[1:].zero_()  # the iteration end re-arms the first counter
 
     def reset_average(self):
         """Start a new weighted average (history slots restart at 0); the grids

@@ -68,7 +68,7 @@ def _compile(src, obj, verbose, extra):
 
 
 JIT_HEADERS = ("vf_device.cuh", "vf_sample.cuh", "vf_vegas_f32.cuh", "vf_plus_args.cuh", "vf_plus_sampler.cuh",
-               "vf_plus_f32.cuh")
+               "vf_plus_f32.cuh", "vf_batch_sampler.cuh")
 
 
 def write_jit_sources():

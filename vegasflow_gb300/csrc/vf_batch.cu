@@ -64,15 +64,19 @@ int vf_batch_blocks(int max_dim, int* blocks, int* smem_bytes) {
   return VF_OK;
 }
 
-int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long long* tile_start,
-                    const int* tile_count, const long long* tile_row, int n_tiles, int max_dim, int* queue,
-                    const unsigned int* calls, const double* grids, const double* params, double* partials,
-                    unsigned long long seed, int* flags, int blocks, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// The sampler arguments shared by vf_batch_sample and vf_batch_sample_jit.
+int batch_args(vf::BatchArgs& a, const vf_batch_item* items, const int* tile_item, const long long* tile_start,
+               const int* tile_count, const long long* tile_row, int n_tiles, int max_dim, int* queue,
+               const unsigned int* calls, const double* grids, const double* params, double* partials,
+               unsigned long long seed, int* flags, int blocks) {
   if (!items || !tile_item || !tile_start || !tile_count || !tile_row || !queue || !calls || !grids ||
       !params || !partials || n_tiles < 0 || blocks < 1)
     return err(VF_ERR_ARG, "vf_batch_sample: NULL buffer or bad sizes");
   if (max_dim < 1 || max_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_batch_sample: max_dim must be 1..16");
-  vf::BatchArgs a;
   a.items = reinterpret_cast<const vf::BatchItem*>(items);
   a.tile_item = tile_item;
   a.tile_start = tile_start;
@@ -93,6 +97,21 @@ int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
   }
+  return VF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long long* tile_start,
+                    const int* tile_count, const long long* tile_row, int n_tiles, int max_dim, int* queue,
+                    const unsigned int* calls, const double* grids, const double* params, double* partials,
+                    unsigned long long seed, int* flags, int blocks, void* stream) {
+  vf::BatchArgs a;
+  const int rc = batch_args(a, items, tile_item, tile_start, tile_count, tile_row, n_tiles, max_dim, queue, calls,
+                            grids, params, partials, seed, flags, blocks);
+  if (rc != VF_OK) return rc;
   const int smem = vf::batch_smem_bytes(max_dim);
   cudaError_t e = set_smem(max_dim, smem);
   if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
@@ -100,6 +119,19 @@ int vf_batch_sample(const vf_batch_item* items, const int* tile_item, const long
   e = cudaLaunchKernel(sample_kernel_for(max_dim), dim3(blocks), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return err(VF_ERR_LAUNCH, cudaGetErrorString(e));
   return launched("vf_batch_sample");
+}
+
+int vf_batch_sample_jit(int integrand_id, const vf_batch_item* items, const int* tile_item,
+                        const long long* tile_start, const int* tile_count, const long long* tile_row, int n_tiles,
+                        int max_dim, int* queue, const unsigned int* calls, const double* grids, const double* params,
+                        double* partials, unsigned long long seed, int* flags, int blocks, void* stream) {
+  vf::BatchArgs a;
+  const int rc = batch_args(a, items, tile_item, tile_start, tile_count, tile_row, n_tiles, max_dim, queue, calls,
+                            grids, params, partials, seed, flags, blocks);
+  if (rc != VF_OK) return rc;
+  const int rl = vf::jit_launch_batch(integrand_id, max_dim, &a, blocks, vf::batch_smem_bytes(max_dim), stream);
+  if (rl != VF_OK) return rl;
+  return launched("vf_batch_sample_jit");
 }
 
 int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, const int* blk_role, int n_blocks,

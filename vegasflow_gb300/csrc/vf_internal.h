@@ -47,6 +47,11 @@ cudaError_t preload_probe_kernels();
 int jit_launch_plus(int integrand_id, int precision, int n_dim, void* args, int rows, int train, bool use_fast,
                     void* stream);
 
+// Launches the NVRTC-compiled batched sampler of a JIT integrand with `args` (a
+// BatchArgs) on `blocks` blocks with `smem` bytes of dynamic shared memory; the
+// integrand must have been compiled for integrals of at least `max_dim` dimensions.
+int jit_launch_batch(int integrand_id, int max_dim, void* args, int blocks, int smem, void* stream);
+
 // Records an error message for vf_last_error_string(); returns `code`.
 int set_error(int code, const char* message);
 

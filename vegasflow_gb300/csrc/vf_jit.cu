@@ -5,7 +5,8 @@
 // (vf_real = the sampler's precision, typedef'd before the source).  It is
 // compiled together with the sampler headers (embedded in the library) into a
 // sampler kernel specialised for the integrand: the fp32 VEGAS kernel on the
-// exact dimension count, or the generic sampler for float64 and plain MC.
+// exact dimension count, the generic sampler for float64 and plain MC, the
+// VEGAS+ samplers, or the batched sampler of a dimension class.
 // The CUBIN is built for sm_103a and loaded with the driver API; launches go
 // through vf_sample with the returned integrand id.
 #include <cuda.h>
@@ -18,6 +19,7 @@
 
 #include "vegasflow_gb300.h"
 #include "vf_internal.h"
+#include "vf_batch_sampler.cuh"
 #include "vf_jit_sources.h"
 #include "vf_plus_f32.cuh"
 #include "vf_plus_sampler.cuh"
@@ -80,7 +82,10 @@ std::string program_text(const char* source, const char* func_name, int alg, int
   src += source;
   src += "\n#define VF_USER_FN " + std::string(func_name) + "\n";
   exprs->clear();
-  if (alg == VF_ALG_PLUS) {
+  if (alg == VF_ALG_BATCH) {
+    src += "#include \"vf_batch_sampler.cuh\"\n";
+    exprs->push_back("vf::vf_batch_sample_kernel<" + std::to_string(n_dim <= 8 ? 8 : 16) + ", true>");
+  } else if (alg == VF_ALG_PLUS) {
     src += "#include \"vf_plus_sampler.cuh\"\n";
     exprs->push_back(std::string("vf::vf_plus_kernel<") + real + ", " + std::to_string(vf::dim_bucket(n_dim)) +
                      ", 99>");
@@ -104,8 +109,8 @@ int compile(const char* source, const char* func_name, int alg, int precision, i
             std::vector<std::string>* lowered, std::string* log) {
   if (!source || !func_name || !*func_name) return VF_ERR_ARG;
   if (n_dim < 1 || n_dim > VF_MAX_DIM) return VF_ERR_UNSUPPORTED;
-  if ((alg != VF_ALG_VEGAS && alg != VF_ALG_PLAIN && alg != VF_ALG_PLUS) ||
-      (precision != VF_PREC_F64 && precision != VF_PREC_F32))
+  if ((alg != VF_ALG_VEGAS && alg != VF_ALG_PLAIN && alg != VF_ALG_PLUS && alg != VF_ALG_BATCH) ||
+      (precision != VF_PREC_F64 && precision != VF_PREC_F32) || (alg == VF_ALG_BATCH && precision != VF_PREC_F32))
     return VF_ERR_ARG;
   std::vector<std::string> exprs;
   const std::string src = program_text(source, func_name, alg, precision, n_dim, &exprs);
@@ -177,6 +182,33 @@ int jit_launch_plus(int integrand_id, int precision, int n_dim, void* args, int 
   }
   void* params[] = {args};
   const CUresult r = drv.launch_kernel(fn, rows, 1, 1, VF_THREADS, 1, 1, smem, (CUstream)stream, params, nullptr);
+  if (r != CUDA_SUCCESS) return set_error(VF_ERR_LAUNCH, "cuLaunchKernel failed for a JIT kernel");
+  return VF_OK;
+}
+
+// Launch a batched JIT sampler for vf_batch_sample_jit (declared in vf_internal.h).
+int jit_launch_batch(int integrand_id, int max_dim, void* args, int blocks, int smem, void* stream) {
+  JitKernel k;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    const int idx = integrand_id - VF_INT_JIT_BASE;
+    if (idx < 0 || idx >= (int)g_kernels.size()) return set_error(VF_ERR_ARG, "unknown JIT integrand id");
+    k = g_kernels[idx];
+  }
+  if (k.alg != VF_ALG_BATCH) return set_error(VF_ERR_ARG, "JIT integrand was not compiled for VF_ALG_BATCH");
+  if (max_dim > (k.n_dim <= 8 ? 8 : 16))
+    return set_error(VF_ERR_ARG, "JIT integrand was compiled for integrals of fewer dimensions");
+  const Driver& drv = driver();
+  if (!drv.ok) return set_error(VF_ERR_CUDA, "CUDA driver entry points unavailable");
+  if (smem > 48 * 1024 && k.smem_set < smem) {
+    if (drv.func_set_attribute(k.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS)
+      return set_error(VF_ERR_CUDA, "cuFuncSetAttribute for a JIT kernel failed");
+    std::lock_guard<std::mutex> lock(g_mu);
+    JitKernel& kk = g_kernels[integrand_id - VF_INT_JIT_BASE];
+    if (kk.smem_set < smem) kk.smem_set = smem;
+  }
+  void* params[] = {args};
+  const CUresult r = drv.launch_kernel(k.fn, blocks, 1, 1, VF_THREADS, 1, 1, smem, (CUstream)stream, params, nullptr);
   if (r != CUDA_SUCCESS) return set_error(VF_ERR_LAUNCH, "cuLaunchKernel failed for a JIT kernel");
   return VF_OK;
 }

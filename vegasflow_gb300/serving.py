@@ -14,9 +14,14 @@ An integral's numbers depend only on itself (its Philox stream id and fixed
 event tiles): a request gives the same result alone and in any mix, up to the
 rounding of the histogram's float atomics.
 
+Integrands are the built-in device integrands, which share one sampler, or
+CUDA-source integrands (``integrands.cuda_integrand``), compiled by NVRTC when
+the request is submitted into a batched sampler of their own: each step then
+launches one sampler per (program, dimension class) present.
+
 Failures stay with the request they concern, never the server: a request that
-cannot be served (unsupported integrand or dimension, larger than the whole
-HBM budget) is rejected at submission; a request can be cancelled, or expire
+cannot be served (unsupported integrand or dimension, CUDA source that does not
+compile, larger than the whole HBM budget) is rejected at submission; a request can be cancelled, or expire
 after its ``timeout``, at the next step boundary; a device allocation that
 fails (growing the partial-row buffer, admitting requests) fails the requests
 it was for and the server carries on with the others.  ``fault_hook``
@@ -28,6 +33,7 @@ expired, rejected, failed) and, for the last three, an ``error``.
 from __future__ import annotations
 
 import ctypes
+import itertools
 import math
 import os
 import time
@@ -40,7 +46,7 @@ from . import _native as nat
 from .utils import preload_kernels
 from .batch import DEFAULT_TILE_EVENTS, ITEM_DTYPE
 from .configflow import BINS_MAX
-from .integrands import DeviceIntegrand
+from .integrands import CudaIntegrand, DeviceIntegrand
 
 MAX_DIM = 16
 PARAMS_PER_SLOT = 2 * MAX_DIM + 2
@@ -67,6 +73,7 @@ class Request:
     status: str = "new"           # waiting, active, then a final status (see the module docstring)
     error: str = ""
     exact: float = field(default=float("nan"), repr=False)
+    program: int = field(default=0, repr=False)  # 0: the built-in sampler; else its batched JIT sampler's id
 
     @property
     def latency(self):
@@ -112,6 +119,25 @@ def step_tables(n_events, n_dim, slots, stream_ids, integrand_ids, grid_off, par
                 n_tiles=total)
 
 
+def launch_groups(act, n_tiles, small_blocks):
+    """The sampler launches of a step over the active requests ``act`` (ordered
+    by (program, n_dim > 8); ``n_tiles`` their tile counts): a list of (first
+    tile, tiles, max_dim, JIT id or None), one per run of equal (program,
+    dimension class).  When the built-in sampler has both classes and one of
+    them has fewer tiles than ``small_blocks`` (the general sampler's persistent
+    grid), they share one launch of the general sampler."""
+    groups = []
+    first = 0
+    for (prog, high), run in itertools.groupby(range(len(act)), key=lambda k: (act[k].program, act[k].n_dim > 8)):
+        count = int(sum(int(n_tiles[k]) for k in run))
+        groups.append((first, count, MAX_DIM if high else 8, prog or None))
+        first += count
+    if (len(groups) >= 2 and groups[0][3] is None and groups[1][3] is None and groups[0][2] == 8
+            and min(groups[0][1], groups[1][1]) < small_blocks):
+        groups[0:2] = [(0, groups[0][1] + groups[1][1], MAX_DIM, None)]
+    return groups
+
+
 def request_footprint(n_dim, n_events, tile_events=DEFAULT_TILE_EVENTS, hist_cap=32):
     """Device bytes a request holds while active: its slot (grid, parameters,
     history, average, counters) and its partial rows."""
@@ -155,7 +181,7 @@ class VegasServer:
         self.avg = torch.zeros((self.max_slots, 5), dtype=torch.float64, device=dev)
         self.iters = torch.zeros(self.max_slots, dtype=torch.int32, device=dev)
         self.calls = torch.zeros(self.max_slots, dtype=torch.int32, device=dev)
-        self._queue = torch.zeros(2, dtype=torch.int32, device=dev)  # one work counter per dimension class
+        self._queue = torch.zeros(4, dtype=torch.int32, device=dev)  # a work counter per sampler launch (grows)
         self._flags = torch.zeros(1, dtype=torch.int32, device=dev)
         self.partials = torch.zeros(1 << 20, dtype=torch.float64, device=dev)
         self._blocks = {}
@@ -202,19 +228,27 @@ class VegasServer:
         now = req.arrival if now is None else now
         reason = ""
         integ = req.integrand
-        if not isinstance(integ, DeviceIntegrand) or not nat.VF_INT_SYMGAUSS <= integ.integrand_id <= nat.VF_INT_SUM:
-            reason = "batched serving takes built-in device integrands"
+        user = isinstance(integ, CudaIntegrand)
+        if not user and (not isinstance(integ, DeviceIntegrand)
+                         or not nat.VF_INT_SYMGAUSS <= integ.integrand_id <= nat.VF_INT_SUM):
+            reason = "batched serving takes built-in device integrands or CUDA-source integrands"
         elif not 1 <= req.n_dim <= MAX_DIM:
             reason = f"n_dim={req.n_dim} outside 1..{MAX_DIM}"
         elif req.n_events < 2:
             reason = f"n_events={req.n_events} < 2"
         elif request_footprint(req.n_dim, req.n_events, self.tile_events, self.hist_cap) > self.hbm_budget:
             reason = "larger than the HBM budget"
+        elif user and integ.params(req.n_dim).size > PARAMS_PER_SLOT:
+            reason = f"more than {PARAMS_PER_SLOT} integrand parameters"
         else:
             try:
                 integ.check_dims(req.n_dim)
+                if user:  # the program's batched sampler for the request's dimension class
+                    req.program = integ.compile_for(nat.VF_ALG_BATCH, nat.VF_PREC_F32, MAX_DIM if req.n_dim > 8 else 8)
             except ValueError as exc:
                 reason = str(exc)
+            except nat.VegasGB300Error as exc:
+                reason = f"the CUDA integrand did not compile: {exc}"
         if reason:
             self._finish(req, "rejected", now, reason)
             return False
@@ -298,14 +332,15 @@ class VegasServer:
     # ---------------------------------------------------------------- one step
     def _tables(self, act):
         return step_tables([r.n_events for r in act], [r.n_dim for r in act], [r.slot for r in act],
-                           [r.rid for r in act], [r.integrand.integrand_id for r in act],
+                           [r.rid for r in act], [r.program or r.integrand.integrand_id for r in act],
                            [r.slot * MAX_DIM * (BINS_MAX + 1) for r in act],
                            [r.slot * PARAMS_PER_SLOT for r in act], self.tile_events)
 
     def step(self, now_fn):
         """Advance every active request by one iteration, then retire finished ones."""
-        # n_dim <= 8 first: those tiles go to the sampler of that dimension class
-        act = sorted(self.active, key=lambda r: r.n_dim > 8)
+        # ordered by (program, dimension class): each run of tiles goes to one
+        # sampler launch (n_dim <= 8: the class with smaller shared tables)
+        act = sorted(self.active, key=lambda r: (r.program, r.n_dim > 8))
         t = self._tables(act)
         if t["rows_total"] > self.partials.numel():
             try:
@@ -327,27 +362,25 @@ class VegasServer:
                 for k in ("tile_item", "tile_start", "tile_count", "tile_row", "blk_item", "blk_role")}
         lib = nat.load()
         s = nat.stream_handle()
-        low = np.array([r.n_dim <= 8 for r in act])
-        n_low = int(t["items"]["n_tiles"][low].sum())
-        n_high = t["n_tiles"] - n_low
-        if n_low and n_high and min(n_low, n_high) < self._blocks[MAX_DIM]:
-            n_low = 0  # a small step: one launch of the general sampler over every tile
-        for first, count, md, q in ((0, n_low, 8, 0), (n_low, t["n_tiles"] - n_low, MAX_DIM, 1)):
-            if count == 0:
-                continue
-            nat.check(lib.vf_batch_sample(nat.ptr(items), nat.ptr(arrs["tile_item"][first:]),
-                                          nat.ptr(arrs["tile_start"][first:]), nat.ptr(arrs["tile_count"][first:]),
-                                          nat.ptr(arrs["tile_row"][first:]), count, md,
-                                          nat.ptr(self._queue[q:q + 1]), nat.ptr(self.calls), nat.ptr(self.grids),
-                                          nat.ptr(self.params), nat.ptr(self.partials), self.seed,
-                                          nat.ptr(self._flags), self._blocks[md], s))
+        groups = launch_groups(act, t["items"]["n_tiles"], self._blocks[MAX_DIM])
+        if len(groups) > self._queue.numel():
+            self._queue = torch.zeros(2 * len(groups), dtype=torch.int32, device=dev)
+        for q, (first, count, md, jit) in enumerate(groups):
+            args = (nat.ptr(items), nat.ptr(arrs["tile_item"][first:]), nat.ptr(arrs["tile_start"][first:]),
+                    nat.ptr(arrs["tile_count"][first:]), nat.ptr(arrs["tile_row"][first:]), count, md,
+                    nat.ptr(self._queue[q:q + 1]), nat.ptr(self.calls), nat.ptr(self.grids), nat.ptr(self.params),
+                    nat.ptr(self.partials), self.seed, nat.ptr(self._flags), self._blocks[md], s)
+            if jit is None:
+                nat.check(lib.vf_batch_sample(*args))
+            else:
+                nat.check(lib.vf_batch_sample_jit(jit, *args))
         nat.check(lib.vf_batch_iteration_end(nat.ptr(items), nat.ptr(arrs["blk_item"]), nat.ptr(arrs["blk_role"]),
                                              int(t["blk_item"].size), nat.ptr(arrs["tile_row"]),
                                              nat.ptr(self.partials), nat.ptr(self.grids), nat.ptr(self.history),
                                              nat.ptr(self.avg), self.hist_cap, nat.ptr(self.iters),
                                              nat.ptr(self.calls), nat.ptr(self._queue), nat.ptr(self._flags), s))
-        if t["n_tiles"] - n_low:
-            self._queue[1:2].zero_()  # the second sampler's counter (the iteration end re-arms the first)
+        if len(groups) > 1:
+            self._queue[1:len(groups)].zero_()  # the other launches' counters (the iteration end re-arms the first)
         slots = torch.as_tensor([r.slot for r in act], dtype=torch.int64, device=dev)
         state = torch.cat([self.avg[slots][:, 2:4].reshape(-1),
                            self.iters[slots].to(torch.float64)]).cpu().numpy()
