@@ -36,8 +36,9 @@ extern "C" {
 #define VF_FLAG_NONFINITE 4       /* a partial sum was NaN or Inf                 */
 #define VF_FLAG_TIMEOUT 8         /* a bounded device-side wait gave up (a copy that
                                      never completed); that launch's sums are partial */
-#define VF_FLAG_HISTORY_FULL 16   /* vf_iteration_dev found no history row left: that
-                                     iteration's result was not recorded              */
+#define VF_FLAG_HISTORY_FULL 16   /* vf_iteration_dev / vf_plus_iteration_dev found no
+                                     history row left: that iteration's result was not
+                                     recorded                                          */
 
 /* ---- constants (configflow.py:13-24) -------------------------------------- */
 #define VF_BINS_MAX 50
@@ -198,6 +199,23 @@ int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, lo
                           const double* partials, int rows, int n_dim, int train, double alpha,
                           double beta, double* grid, double* hist_out, double* arr_var_out,
                           double* history, double* avg, int iter, int* flags, void* stream);
+
+/*
+ * One whole VEGAS+ iteration with device-side counters, for capture in a CUDA
+ * graph (vflowplus.py:187-241 per replay): vf_plus_sample with Philox uniforms,
+ * the call counter read from *call_dev, then vf_plus_iteration_end (train: the
+ * refinement of `precision`) with the iteration index read from *iter_dev, after
+ * which both advance by one.  history has hist_cap rows (VF_FLAG_HISTORY_FULL
+ * when the index reaches it).  The adaptive reallocation stays on the device, so
+ * replays need no host work between iterations.
+ */
+int vf_plus_iteration_dev(int precision, double* grid, int n_dim, int n_strat, int n_hcubes, int* n_ev,
+                          long long* ev_start, double xjac, const double* xmin, const double* xdelta,
+                          double xdeltajac, unsigned long long seed, unsigned int* call_dev, int* iter_dev,
+                          int integrand, const double* params, int train, int adaptive, int min_neval,
+                          double init_calls, double alpha, double beta, double* ress, double* ress2,
+                          double* partials, int rows, double* history, int hist_cap, double* avg, int* flags,
+                          void* stream);
 
 /*
  * Batched VEGAS (no counterpart in the reference, which integrates one

@@ -1,15 +1,17 @@
 """CUDA-graph iterations (``cuda_graph=True``): one captured vf_iteration_dev
-replayed per iteration, the Philox call counter and the history row advancing
-on the device.  The replays run the same kernels on the same events as the
-eager iterations, so results agree to the histogram atomics' rounding."""
+(VegasFlowPlus: vf_plus_iteration_dev) replayed per iteration, the Philox call
+counter and the history row advancing on the device.  The replays run the same
+kernels on the same events as the eager iterations, so results agree to the
+histogram atomics' rounding."""
 
 import ctypes
+import math
 
 import numpy as np
 import pytest
 import torch
 
-from vegasflow_gb300 import PlainFlow, VegasFlow, integrands, _native as nat
+from vegasflow_gb300 import PlainFlow, VegasFlow, VegasFlowPlus, integrands, _native as nat
 
 pytestmark = pytest.mark.gpu
 
@@ -80,6 +82,38 @@ def test_plain_graph_matches_eager(precision):
 def test_jit_integrand_graph_matches_eager():
     f = integrands.cuda_integrand(CAMEL, "camel", params=[0.3, 0.7, 0.2])
     eager, graph = _pair(VegasFlow, "fp32", f, n_dim=3)
+    np.testing.assert_allclose(graph.run_integration(4), eager.run_integration(4), rtol=2e-6)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_plus_graph_matches_eager(precision, adaptive):
+    """VegasFlowPlus replays: the adaptive reallocation (n_ev, ev_start) stays on
+    the device between iterations, and the host reads the new event count only
+    when asked."""
+    eager, graph = _pair(VegasFlowPlus, precision, integrands.symgauss(0.2), n_dim=3, n=200_000,
+                         adaptive=adaptive)
+    n0 = graph.n_events
+    for _ in range(2):  # the second run replays the same graph
+        r_e = eager.run_integration(4)
+        r_g = graph.run_integration(4)
+        np.testing.assert_allclose(r_g, r_e, rtol=_rtol(precision))
+    g1 = graph._graph
+    assert g1 is not None and graph._call_ctr == eager._call_ctr == 8 and len(graph._history) == 8
+    np.testing.assert_allclose(graph.n_ev.cpu().numpy(), eager.n_ev.cpu().numpy(), rtol=0, atol=1)
+    assert abs(graph.n_events - eager.n_events) <= graph.n_hypercubes
+    if adaptive:
+        assert graph.n_events != n0  # reallocated on the device
+    np.testing.assert_allclose(graph.divisions.cpu().numpy(), eager.divisions.cpu().numpy(), rtol=0,
+                               atol=1e-12 if precision == "fp64" else 1e-6)
+    graph.run_integration(2)
+    assert graph._graph is g1  # reading n_events does not force a new capture
+    assert abs(r_g[0] - math.erf(2.5) ** 3) < 5 * r_g[1]
+
+
+def test_plus_jit_integrand_graph_matches_eager():
+    f = integrands.cuda_integrand(CAMEL, "camel", params=[0.3, 0.7, 0.2])
+    eager, graph = _pair(VegasFlowPlus, "fp32", f, n_dim=3, adaptive=True)
     np.testing.assert_allclose(graph.run_integration(4), eager.run_integration(4), rtol=2e-6)
 
 

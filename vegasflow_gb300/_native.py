@@ -77,6 +77,8 @@ SIGNATURES = {
     "vf_plus_reduce_events": [_I, _P, _P, _P, _P, _P, _I, _I, _I, _P, _P, _P, _I, _P],
     "vf_plus_iteration_end": [_P, _P, _P, _P, _I, _I, _I, _D, _P, _I, _I, _I, _D, _D, _P, _P, _P, _P,
                               _P, _I, _P, _P],
+    "vf_plus_iteration_dev": [_I, _P, _I, _I, _I, _P, _P, _D, _P, _P, _D, _U64, _P, _P, _I, _P, _I, _I, _I, _D,
+                              _D, _D, _P, _P, _P, _I, _P, _I, _P, _P, _P],
     "vf_batch_blocks": [_I, _P, _P],
     "vf_batch_sample": [_P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],
     "vf_batch_sample_jit": [_I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],

@@ -72,12 +72,17 @@ int vf_plus_rows(int precision, int n_dim, int n_hcubes, int* rows) {
   return VF_OK;
 }
 
-int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, int n_hcubes,
-                   const int* n_ev, const long long* ev_start, double xjac, const double* xmin,
-                   const double* xdelta, double xdeltajac, const double* u_inj,
-                   unsigned long long seed, unsigned int call_ctr, int integrand, const double* params,
-                   int train, double* ress, double* ress2, double* partials, int rows, int* ind_out,
-                   void* x_out, void* w_out, int* flags, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// vf_plus_sample with, optionally, the Philox call counter in device memory.
+int plus_sample_impl(int precision, const double* grid, int n_dim, int n_strat, int n_hcubes, const int* n_ev,
+                     const long long* ev_start, double xjac, const double* xmin, const double* xdelta,
+                     double xdeltajac, const double* u_inj, unsigned long long seed, unsigned int call_ctr,
+                     const unsigned int* call_dev, int integrand, const double* params, int train, double* ress,
+                     double* ress2, double* partials, int rows, int* ind_out, void* x_out, void* w_out, int* flags,
+                     void* stream) {
   if (precision != VF_PREC_F64 && precision != VF_PREC_F32) return err(VF_ERR_ARG, "vf_plus_sample: precision");
   if (n_dim < 1 || n_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_plus_sample: n_dim must be 1..16");
   if (!grid || !n_ev || !ev_start || n_strat < 1 || n_hcubes < 1 || rows < 1)
@@ -124,6 +129,7 @@ int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, in
   }
   for (int q = 0; q < 8; ++q) a.ctr2[q] = (call_ctr << 4) | (unsigned int)q;
   a.ctr3 = call_ctr >> 28;
+  a.call_dev = call_dev;
   if (jit) {
     const bool fast = precision == VF_PREC_F32 && !u_inj && !ind_out && !x_out && !w_out;
     const int rc = vf::jit_launch_plus(integrand, precision, n_dim, &a, rows, a.train, fast, stream);
@@ -135,6 +141,68 @@ int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, in
   const cudaError_t e = cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return err(VF_ERR_LAUNCH, cudaGetErrorString(e));
   return launched("vf_plus_sample");
+}
+
+// vf_plus_iteration_end with, optionally, the iteration index and the Philox
+// call counter in device memory (read, then advanced).
+int plus_end_impl(const double* ress, const double* ress2, int* n_ev, long long* ev_start, int n_hcubes, int adaptive,
+                  int min_neval, double init_calls, const double* partials, int rows, int n_dim, int train,
+                  double alpha, double beta, double* grid, double* hist_out, double* arr_var_out, double* history,
+                  double* avg, int iter, int* iter_dev, unsigned int* call_dev, int hist_cap, int* flags,
+                  void* stream) {
+  if (!ress || !ress2 || !n_ev || !ev_start || !history || !avg || n_hcubes < 1 || iter < 0)
+    return err(VF_ERR_ARG, "vf_plus_iteration_end: NULL buffer");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_plus_iteration_end: n_dim");
+  if ((train || hist_out) && (!partials || rows < 1)) return err(VF_ERR_ARG, "vf_plus_iteration_end: partials");
+  if (train && !grid) return err(VF_ERR_ARG, "vf_plus_iteration_end: grid required when train");
+  if (adaptive && min_neval < 1) return err(VF_ERR_ARG, "vf_plus_iteration_end: min_neval");
+  if (n_hcubes > VF_PEND_CLUSTER * VF_PEND_THREADS * VF_PEND_MAXC)
+    return err(VF_ERR_UNSUPPORTED, "vf_plus_iteration_end: more than 16384 hypercubes");
+  if (train < 0 || train > 2) return err(VF_ERR_ARG, "vf_plus_iteration_end: train must be 0, 1 or 2");
+  if (iter_dev && hist_cap < 1) return err(VF_ERR_ARG, "vf_plus_iteration_end: hist_cap");
+  vf::PlusEndArgs a;
+  a.ress = ress;
+  a.ress2 = ress2;
+  a.n_ev = n_ev;
+  a.ev_start = ev_start;
+  a.arr_var = arr_var_out;
+  a.partials = partials;
+  a.grid = grid;
+  a.hist_out = hist_out;
+  a.history = history;
+  a.avg = avg;
+  a.flags = flags;
+  a.init_calls = init_calls;
+  a.alpha = alpha;
+  a.beta = beta;
+  a.n_hcubes = n_hcubes;
+  a.min_neval = min_neval;
+  a.adaptive = adaptive ? 1 : 0;
+  a.rows = rows;
+  a.n_dim = n_dim;
+  a.train = train;
+  a.iter = iter;
+  a.iter_dev = iter_dev;
+  a.call_dev = call_dev;
+  a.hist_cap = hist_cap;
+  const int clusters = (a.train || hist_out) ? n_dim + 1 : 1;
+  vf::vf_plus_iteration_end_kernel<<<clusters * VF_PEND_CLUSTER, VF_PEND_THREADS, 0, (cudaStream_t)stream>>>(a);
+  return launched("vf_plus_iteration_end");
+}
+
+}  // namespace
+
+extern "C" {
+
+int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, int n_hcubes,
+                   const int* n_ev, const long long* ev_start, double xjac, const double* xmin,
+                   const double* xdelta, double xdeltajac, const double* u_inj,
+                   unsigned long long seed, unsigned int call_ctr, int integrand, const double* params,
+                   int train, double* ress, double* ress2, double* partials, int rows, int* ind_out,
+                   void* x_out, void* w_out, int* flags, void* stream) {
+  return plus_sample_impl(precision, grid, n_dim, n_strat, n_hcubes, n_ev, ev_start, xjac, xmin, xdelta, xdeltajac,
+                          u_inj, seed, call_ctr, nullptr, integrand, params, train, ress, ress2, partials, rows,
+                          ind_out, x_out, w_out, flags, stream);
 }
 
 int vf_plus_reduce_events(int precision, const void* f, const void* w, const int* ind, const int* n_ev,
@@ -171,40 +239,28 @@ int vf_plus_iteration_end(const double* ress, const double* ress2, int* n_ev, lo
                           const double* partials, int rows, int n_dim, int train, double alpha,
                           double beta, double* grid, double* hist_out, double* arr_var_out,
                           double* history, double* avg, int iter, int* flags, void* stream) {
-  if (!ress || !ress2 || !n_ev || !ev_start || !history || !avg || n_hcubes < 1 || iter < 0)
-    return err(VF_ERR_ARG, "vf_plus_iteration_end: NULL buffer");
-  if (n_dim < 1 || n_dim > VF_MAX_DIM) return err(VF_ERR_UNSUPPORTED, "vf_plus_iteration_end: n_dim");
-  if ((train || hist_out) && (!partials || rows < 1)) return err(VF_ERR_ARG, "vf_plus_iteration_end: partials");
-  if (train && !grid) return err(VF_ERR_ARG, "vf_plus_iteration_end: grid required when train");
-  if (adaptive && min_neval < 1) return err(VF_ERR_ARG, "vf_plus_iteration_end: min_neval");
-  if (n_hcubes > VF_PEND_CLUSTER * VF_PEND_THREADS * VF_PEND_MAXC)
-    return err(VF_ERR_UNSUPPORTED, "vf_plus_iteration_end: more than 16384 hypercubes");
-  if (train < 0 || train > 2) return err(VF_ERR_ARG, "vf_plus_iteration_end: train must be 0, 1 or 2");
-  vf::PlusEndArgs a;
-  a.ress = ress;
-  a.ress2 = ress2;
-  a.n_ev = n_ev;
-  a.ev_start = ev_start;
-  a.arr_var = arr_var_out;
-  a.partials = partials;
-  a.grid = grid;
-  a.hist_out = hist_out;
-  a.history = history;
-  a.avg = avg;
-  a.flags = flags;
-  a.init_calls = init_calls;
-  a.alpha = alpha;
-  a.beta = beta;
-  a.n_hcubes = n_hcubes;
-  a.min_neval = min_neval;
-  a.adaptive = adaptive ? 1 : 0;
-  a.rows = rows;
-  a.n_dim = n_dim;
-  a.train = train;
-  a.iter = iter;
-  const int clusters = (a.train || hist_out) ? n_dim + 1 : 1;
-  vf::vf_plus_iteration_end_kernel<<<clusters * VF_PEND_CLUSTER, VF_PEND_THREADS, 0, (cudaStream_t)stream>>>(a);
-  return launched("vf_plus_iteration_end");
+  return plus_end_impl(ress, ress2, n_ev, ev_start, n_hcubes, adaptive, min_neval, init_calls, partials, rows, n_dim,
+                       train, alpha, beta, grid, hist_out, arr_var_out, history, avg, iter, nullptr, nullptr, 0, flags,
+                       stream);
+}
+
+int vf_plus_iteration_dev(int precision, double* grid, int n_dim, int n_strat, int n_hcubes, int* n_ev,
+                          long long* ev_start, double xjac, const double* xmin, const double* xdelta,
+                          double xdeltajac, unsigned long long seed, unsigned int* call_dev, int* iter_dev,
+                          int integrand, const double* params, int train, int adaptive, int min_neval,
+                          double init_calls, double alpha, double beta, double* ress, double* ress2,
+                          double* partials, int rows, double* history, int hist_cap, double* avg, int* flags,
+                          void* stream) {
+  if (!call_dev || !iter_dev) return err(VF_ERR_ARG, "vf_plus_iteration_dev: call_dev and iter_dev are required");
+  if (integrand == VF_INT_NONE) return err(VF_ERR_ARG, "vf_plus_iteration_dev: needs an integrand");
+  int rc = plus_sample_impl(precision, grid, n_dim, n_strat, n_hcubes, n_ev, ev_start, xjac, xmin, xdelta, xdeltajac,
+                            nullptr, seed, 0, call_dev, integrand, params, train, ress, ress2, partials, rows, nullptr,
+                            nullptr, nullptr, flags, stream);
+  if (rc) return rc;
+  const int tr = train ? (precision == VF_PREC_F32 ? 2 : 1) : 0;
+  return plus_end_impl(ress, ress2, n_ev, ev_start, n_hcubes, adaptive, min_neval, init_calls, partials, rows, n_dim,
+                       tr, alpha, beta, grid, nullptr, nullptr, history, avg, 0, iter_dev, call_dev, hist_cap, flags,
+                       stream);
 }
 
 }  // extern "C"

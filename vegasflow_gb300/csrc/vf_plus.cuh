@@ -105,6 +105,12 @@ struct PlusEndArgs {
   int n_dim;
   int train;
   int iter;
+  // nullable: the iteration index in device memory, read here (instead of
+  // `iter`) and then advanced with the Philox call counter `call_dev` for the
+  // next iteration (a launch replayed from a CUDA graph); history has hist_cap rows
+  int* iter_dev;
+  unsigned int* call_dev;
+  int hist_cap;
 };
 
 // var^(beta/2), vflowplus.py:157.  For the default beta = 3/4 the power 3/8 is
@@ -215,6 +221,7 @@ vf_plus_iteration_end_kernel(const PlusEndArgs a) {
   cluster.sync();
   __shared__ double all[3];  // the cluster's totals, added in rank order in every block
   __shared__ double s_mean;
+  __shared__ int s_it, s_room;  // the iteration index; whether its history row exists
   if (t == 0) {
     double c1 = 0.0, c2 = 0.0, c3 = 0.0;
     for (int r = 0; r < VF_PEND_CLUSTER; ++r) {
@@ -227,25 +234,39 @@ vf_plus_iteration_end_kernel(const PlusEndArgs a) {
     all[1] = c2;
     all[2] = c3;
     if (rank == 0) {
-      const double res = c1;
-      const double sigma = sqrt(c2);
-      double* hrow = a.history + (long long)a.iter * 2;
-      hrow[0] = res;
-      hrow[1] = sigma;
-      const double wgt = 1.0 / __dmul_rn(sigma, sigma);
-      a.avg[0] = __dadd_rn(a.avg[0], __dmul_rn(res, wgt));
-      a.avg[1] = __dadd_rn(a.avg[1], wgt);
-      const double mean = a.avg[0] / a.avg[1];
-      a.avg[2] = mean;
-      a.avg[3] = sqrt(1.0 / a.avg[1]);
-      s_mean = mean;
-      if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+      const int it = a.iter_dev ? *a.iter_dev : a.iter;
+      s_it = it;
+      s_room = it >= 0 && (!a.iter_dev || it < a.hist_cap);
+      if (!s_room) {  // no history row left: report; the average is left as it was
+        if (a.flags) atomicOr(a.flags, VF_FLAG_HISTORY_FULL);
+      } else {
+        const double res = c1;
+        const double sigma = sqrt(c2);
+        double* hrow = a.history + (long long)it * 2;
+        hrow[0] = res;
+        hrow[1] = sigma;
+        const double wgt = 1.0 / __dmul_rn(sigma, sigma);
+        a.avg[0] = __dadd_rn(a.avg[0], __dmul_rn(res, wgt));
+        a.avg[1] = __dadd_rn(a.avg[1], wgt);
+        const double mean = a.avg[0] / a.avg[1];
+        a.avg[2] = mean;
+        a.avg[3] = sqrt(1.0 / a.avg[1]);
+        s_mean = mean;
+        if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+      }
     }
   }
   __syncthreads();
-  if (rank == 0) {
-    const double chi2 = block_chi2(a.history, 2, 1, a.iter + 1, s_mean);
-    if (t == 0) a.avg[4] = a.iter > 0 ? chi2 / a.iter : 0.0;
+  if (rank == 0 && s_room) {
+    const int it = s_it;
+    const double chi2 = block_chi2(a.history, 2, 1, it + 1, s_mean);
+    if (t == 0) {
+      a.avg[4] = it > 0 ? chi2 / it : 0.0;
+      if (a.iter_dev) {  // the next iteration's index and Philox call (the sampler has run: stream order)
+        *a.iter_dev = it + 1;
+        if (a.call_dev) *a.call_dev += 1u;
+      }
+    }
   }
   if (!a.adaptive) {
     cluster.sync();  // the other blocks' totals stay readable until every block has read them

@@ -56,6 +56,8 @@ __global__ void __launch_bounds__(VF_THREADS) vf_plus_f32_kernel(const PlusArgs 
   IntegrandConsts<float, D> kc;
   load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
   float* my_hist = hist + warp * NB;
+  u32 cw2, cw3;
+  plus_call_words(a, cw2, cw3);
   const u32 ns = (u32)a.n_strat;
   const float inv_ns = 1.0f / (float)ns;
   double blk1 = 0.0, blk2 = 0.0;
@@ -83,7 +85,7 @@ __global__ void __launch_bounds__(VF_THREADS) vf_plus_f32_kernel(const PlusArgs 
       float wf = 1.0f;
 #pragma unroll
       for (int q = 0; q < (D + 3) / 4; ++q) {
-        u32 c0 = (u32)e, c1 = (u32)(e >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+        u32 c0 = (u32)e, c1 = (u32)(e >> 32), c2 = cw2 | (u32)q, c3 = cw3;
         philox4x32_10_rk(c0, c1, c2, c3, a.rk);
         const u32 wq[4] = {c0, c1, c2, c3};
 #pragma unroll

@@ -27,6 +27,8 @@ __global__ void __launch_bounds__(VF_THREADS) vf_plus_kernel(const PlusArgs a) {
   const double inv_strat = 1.0 / (double)a.n_strat;
   int bad = 0;
   double blk1 = 0.0, blk2 = 0.0;  // this warp's contribution to the block row (lane 0)
+  u32 cw2, cw3;
+  plus_call_words(a, cw2, cw3);
 
   const int gwarp = blockIdx.x * (blockDim.x >> 5) + warp;
   const int nwarps = gridDim.x * (blockDim.x >> 5);
@@ -58,7 +60,7 @@ __global__ void __launch_bounds__(VF_THREADS) vf_plus_kernel(const PlusArgs a) {
 #pragma unroll
         for (int q = 0; q < (DMAX + 1) / 2; ++q)
           if (2 * q < D) {
-            u32 c0 = (u32)e, c1 = (u32)((u64)e >> 32), c2 = a.ctr2[q], c3 = a.ctr3;
+            u32 c0 = (u32)e, c1 = (u32)((u64)e >> 32), c2 = cw2 | (u32)q, c3 = cw3;
             philox4x32_10_rk(c0, c1, c2, c3, a.rk);
             u[2 * q] = tech_cut(u53(c0, c1));
             if (2 * q + 1 < DMAX) u[2 * q + 1] = tech_cut(u53(c2, c3));

@@ -563,6 +563,17 @@ class MonteCarloFlow(ABC):
                  nat.ptr(ws["history"]), int(ws["history"].shape[0]), nat.ptr(ws["avg"]), nat.ptr(ws["flags"]),
                  nat.stream_handle())
 
+    def _graph_signature(self, ws):
+        """Every value the captured call was made with: a change means a new capture."""
+        def addr(p):
+            return p.value if p is not None else 0
+
+        xmin, xdelta, xdj = self._limits_ptrs()
+        return (self._ALG, self._prec, addr(self._grid_ptr()), self.n_events, self.xjac, self._seed, self._int_id,
+                self._params_dev.data_ptr(), bool(self._train_now()), self._rows, ws["partials"].data_ptr(),
+                ws["history"].data_ptr(), ws["history"].shape[0], ws["avg"].data_ptr(), ws["flags"].data_ptr(),
+                ws["counters"].data_ptr(), addr(xmin), addr(xdelta), xdj, self._shape)
+
     def _graph_for(self, n_iter):
         """The CUDA graph of one iteration (captured again whenever an argument
         of the captured call changed), with room for ``n_iter`` history rows."""
@@ -573,14 +584,7 @@ class MonteCarloFlow(ABC):
         if "counters" not in ws:
             ws["counters"] = torch.zeros(2, dtype=torch.int32, device=self.device)
         self._apply_shape()
-        def addr(p):
-            return p.value if p is not None else 0
-
-        xmin, xdelta, xdj = self._limits_ptrs()
-        key = (self._ALG, self._prec, addr(self._grid_ptr()), self.n_events, self.xjac, self._seed, self._int_id,
-               self._params_dev.data_ptr(), bool(self._train_now()), self._rows, ws["partials"].data_ptr(),
-               ws["history"].data_ptr(), ws["history"].shape[0], ws["avg"].data_ptr(), ws["flags"].data_ptr(),
-               ws["counters"].data_ptr(), addr(xmin), addr(xdelta), xdj, self._shape)
+        key = self._graph_signature(ws)
         if self._graph is None or self._graph_key != key:
             from .utils import preload_kernels
             preload_kernels(self.device)
@@ -616,9 +620,9 @@ class MonteCarloFlow(ABC):
     def run_integration(self, n_iter, log_time=True, histograms=None):
         """Run ``n_iter`` iterations; returns (result, sigma) (monte_carlo.py:645-741).
 
-        With ``cuda_graph=True`` (device integrands, VegasFlow and PlainFlow) the
-        iterations are replays of one captured CUDA graph (two kernels, no host
-        work between iterations)."""
+        With ``cuda_graph=True`` (device integrands; VegasFlow, PlainFlow and
+        VegasFlowPlus) the iterations are replays of one captured CUDA graph (two
+        kernels, no host work between iterations)."""
         self._require_gpu()
         self._reset_average()
         first = len(self._history)

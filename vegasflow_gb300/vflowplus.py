@@ -46,7 +46,7 @@ class VegasFlowPlus(VegasFlow):
     """VEGAS+ (vflowplus.py:83)."""
 
     _FUSED_F32_SAMPLER = False  # samples per hypercube through its own kernels
-    _GRAPH_ITERATIONS = False
+    _GRAPH_ITERATIONS = True  # one iteration is vf_plus_iteration_dev (CUDA-graph replayable)
 
     def __init__(self, n_dim, n_events, train=True, adaptive=False, events_limit=None, **kwargs):
         if events_limit is None:  # vflowplus.py:89-99
@@ -215,6 +215,36 @@ class VegasFlowPlus(VegasFlow):
         row = ws["history"][self._it]
         self._it += 1
         return row[0], row[1]
+
+    # ---------------------------------------------------------------- CUDA-graph iterations
+    def _graph_signature(self, ws):
+        def addr(p):
+            return p.value if p is not None else 0
+
+        ws = self._plus_buffers()  # allocated before any capture
+        xmin, xdelta, xdj = self._limits_ptrs()
+        return ("plus", self._prec, self.divisions.data_ptr(), self.n_ev.data_ptr(), self._ev_start.data_ptr(),
+                self.xjac, self._seed, self._int_id, self._params_dev.data_ptr(), bool(self.train), self._adaptive,
+                self._rows, ws["partials"].data_ptr(), ws["ress"].data_ptr(), ws["ress2"].data_ptr(),
+                ws["history"].data_ptr(), ws["history"].shape[0], ws["avg"].data_ptr(), ws["flags"].data_ptr(),
+                ws["counters"].data_ptr(), addr(xmin), addr(xdelta), xdj)
+
+    def _graph_call(self, ws):
+        ws = self._plus_buffers()
+        xmin, xdelta, xdj = self._limits_ptrs()
+        nat.call("vf_plus_iteration_dev", self._prec, nat.ptr(self.divisions), self.n_dim, self._n_strat,
+                 self._n_hcubes, nat.ptr(self.n_ev), nat.ptr(self._ev_start), float(self.xjac), xmin, xdelta,
+                 float(xdj), self._seed, nat.ptr(ws["counters"][0:1]), nat.ptr(ws["counters"][1:2]),
+                 int(self._int_id), nat.ptr(self._params_dev), int(bool(self.train)), int(self._adaptive),
+                 int(self.min_neval_hcube), float(self._init_calls), float(ALPHA), float(BETA),
+                 nat.ptr(ws["ress"]), nat.ptr(ws["ress2"]), nat.ptr(ws["partials"]), self._rows,
+                 nat.ptr(ws["history"]), int(ws["history"].shape[0]), nat.ptr(ws["avg"]), nat.ptr(ws["flags"]),
+                 nat.stream_handle())
+
+    def _run_graph(self, n_iter, log_time):
+        super()._run_graph(n_iter, log_time)
+        if self._adaptive:
+            self._n_ev_stale = True  # the replays reallocated on the device
 
     def _iteration_content(self):
         """vflowplus.py:222-241: sample, sums, sigma, reallocation, refinement."""
