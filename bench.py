@@ -78,6 +78,10 @@ def _parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 1,024-integral batched run")
     ap.add_argument("--no-injected", action="store_true",
                     help="skip the injected-uniform (HBM-streaming) measurement")
+    ap.add_argument("--case", choices=["configs", "c4", "sampler", "injected"],
+                    help="run only this workload and print its record (for profiling one kernel family): "
+                         "configs = C1 and C3, c4 = the 1,024-integral batch (fp32 only), sampler = "
+                         "generate_random_array, injected = streamed float64 uniforms")
     return ap.parse_args()
 
 
@@ -260,6 +264,13 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     exact = math.erf(0.5 / A_WIDTH) ** N_DIM
     K, W = args.steps, max(3, args.warmup)
+    if args.case:
+        run_case = {"configs": lambda: configs_run(dev), "c4": lambda: batched_run(dev, fp64_sample=False),
+                    "sampler": lambda: sampler_run(dev, args.events, K, W),
+                    "injected": lambda: injected_run(dev, args.events, K, W)}[args.case]
+        if rank == 0:
+            print(json.dumps({"case": args.case, "result": run_case()}), flush=True)
+        return
 
     def timed_run(precision, seed):
         """W warm-up + K timed iterations; returns per-iteration and sampler times (s)."""
@@ -428,7 +439,7 @@ def injected_run(dev, n_events, K, W, seed=11):
     step_ms = [a.elapsed_time(c) for a, b, c in marks]
     samp_ms = [a.elapsed_time(b) for a, b, c in marks]
     first = inst._workspace()["history"][0].cpu().numpy()
-    flags = int(inst._workspace()["flags"].item())
+    flags = int(inst._workspace()["flags"][0].item())
     del u
     torch.cuda.empty_cache()
     samp = statistics.mean(samp_ms) / 1e3
@@ -510,7 +521,8 @@ def configs_run(dev):
     """The other configurations of the metric, briefly: C1 (4-D Gaussian,
     float64, 1e6 events x 5 iterations, seed 7) and C3 (VegasFlowPlus adaptive,
     6-D Breit-Wigner x linear, 2e6 events x 10 iterations) in both precisions,
-    each against its exact value."""
+    each against its exact value, with eager iterations and with CUDA-graph
+    replays (``cuda_graph=True``); ``events_per_s`` is the faster of the two."""
     import numpy as np
     import torch
 
@@ -521,25 +533,34 @@ def configs_run(dev):
     coeffs = np.random.default_rng(3).random(5)
     exact3 = integrands.breit_wigner_exact(6, coeffs)
     for name, make, it, exact in (
-            ("C1", lambda p: (VegasFlow(4, 1_000_000, verbose=False, precision=p, seed=7, device=dev),
-                              integrands.symgauss(A_WIDTH)), 5, exact1),
-            ("C3", lambda p: (VegasFlowPlus(6, 2_000_000, adaptive=True, verbose=False, precision=p, seed=7,
-                                            device=dev), integrands.breit_wigner(coeffs)), 10, exact3)):
+            ("C1", lambda p, g: (VegasFlow(4, 1_000_000, verbose=False, precision=p, seed=7, device=dev,
+                                           cuda_graph=g), integrands.symgauss(A_WIDTH)), 5, exact1),
+            ("C3", lambda p, g: (VegasFlowPlus(6, 2_000_000, adaptive=True, verbose=False, precision=p, seed=7,
+                                               device=dev, cuda_graph=g), integrands.breit_wigner(coeffs)),
+             10, exact3)):
         for prec in ("fp64", "fp32"):
-            inst, f = make(prec)
-            inst.compile(f)
-            inst.run_integration(1)  # warm-up (compile-time work, first launches)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            res, sig = inst.run_integration(it)
-            dt = time.perf_counter() - t0
-            events = sum(int(h) for h in [inst.n_events] * it)
-            out[f"{name}_{prec}"] = {"events_per_s": events / dt, "seconds": dt, "mean": float(res),
-                                     "sigma": float(sig), "pull_vs_exact": (float(res) - exact) / float(sig)}
+            row = {}
+            for graph in (False, True):
+                inst, f = make(prec, graph)
+                inst.compile(f)
+                inst.run_integration(it)  # warm-up: compile-time work, first launches, the graph capture
+                n0 = inst.n_events
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                res, sig = inst.run_integration(it)
+                dt = time.perf_counter() - t0
+                # VegasFlowPlus reallocates every iteration: the mean of the counts before and after
+                events = it * (n0 + inst.n_events) / 2
+                key = "graph" if graph else "eager"
+                row[key] = {"events_per_s": events / dt, "seconds": dt, "mean": float(res), "sigma": float(sig),
+                            "pull_vs_exact": (float(res) - exact) / float(sig)}
+            best = max(row, key=lambda k: row[k]["events_per_s"])
+            out[f"{name}_{prec}"] = dict(row[best], iterations=best, eager_events_per_s=row["eager"]["events_per_s"],
+                                         graph_events_per_s=row["graph"]["events_per_s"])
     return out
 
 
-def batched_run(dev, n_iter=5):
+def batched_run(dev, n_iter=5, fp64_sample=True):
     """C4: 1,024 Gaussians (dims 2-16, 1e4-1e7 events) with their own grids, 5
     iterations as CUDA-graph replays of the batched fp32 engine, against the
     float64 single-integral path run one integral after another on a sample."""
@@ -561,6 +582,12 @@ def batched_run(dev, n_iter=5):
     torch.cuda.synchronize()
     t = a.elapsed_time(c) / 1e3
     ev = b.total_events() * n_iter
+    out = {"workload": "1,024 Gaussians, dims 2-16, 1e4-1e7 events/iteration, own grids, 5 iterations",
+           "integrals": len(specs), "events_per_iteration": b.total_events(),
+           "fp32_batched_events_per_s": ev / t, "ms_per_iteration": 1e3 * t / n_iter,
+           "graph": True, "launches_per_iteration": 2}
+    if not fp64_sample:
+        return out
     # float64 one by one, on every 16th integral (64 of them)
     sample = specs[::16]
     torch.cuda.synchronize()
@@ -572,12 +599,9 @@ def batched_run(dev, n_iter=5):
     torch.cuda.synchronize()
     t64 = time.perf_counter() - t0
     ev64 = sum(n for _, n, _ in sample) * n_iter
-    return {"workload": "1,024 Gaussians, dims 2-16, 1e4-1e7 events/iteration, own grids, 5 iterations",
-            "integrals": len(specs), "events_per_iteration": b.total_events(),
-            "fp32_batched_events_per_s": ev / t, "ms_per_iteration": 1e3 * t / n_iter,
-            "graph": True, "launches_per_iteration": 2,
-            "fp64_one_by_one_events_per_s": ev64 / t64,
-            "fp64_sample": f"{len(sample)} of the 1,024 integrals, run_integration({n_iter}) each"}
+    out.update({"fp64_one_by_one_events_per_s": ev64 / t64,
+                "fp64_sample": f"{len(sample)} of the 1,024 integrals, run_integration({n_iter}) each"})
+    return out
 
 
 def serving_run(seconds):

@@ -123,7 +123,8 @@ int vf_reduce_events(int precision, const void* f, const void* w, const int* ind
 /*
  * Iteration end: fixed-order sum of the partial rows, sigma
  * (vflow.py:437-438), history[iter] = (res, sigma), the running
- * 1/sigma^2-weighted mean, its sigma and chi^2/dof in avg[n_out][5]
+ * 1/sigma^2-weighted mean, its sigma and chi^2/dof in avg[n_out][5] (iter = 0
+ * starts a new average: avg's previous contents are not read)
  * (monte_carlo.py:712-732), and -- when train -- refine_grid (vflow.py:349-362,
  * refine_grid_per_dimension vflow.py:135-211) on `grid` in place: train = 1
  * refines in float64 (the reference's default arithmetic), train = 2 in float32

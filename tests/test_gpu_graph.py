@@ -117,6 +117,29 @@ def test_plus_jit_integrand_graph_matches_eager():
     np.testing.assert_allclose(graph.run_integration(4), eager.run_integration(4), rtol=2e-6)
 
 
+def test_capture_survives_garbage_graphs():
+    """Unreachable integrators that hold CUDA graphs (in reference cycles) do not
+    break a later capture: the collector runs before it, never inside it (the
+    reset of a graph is not permitted while a stream captures)."""
+    import gc
+
+    old = gc.get_threshold()
+    try:
+        for seed in range(3):
+            a = VegasFlow(2, 10_000, verbose=False, seed=seed, cuda_graph=True)
+            a.compile(integrands.symgauss())
+            a.run_integration(2)
+            a._cycle = a  # left to the cyclic collector
+            del a
+        gc.set_threshold(1, 1, 1)  # a collection at almost every allocation
+        b = VegasFlow(2, 10_000, verbose=False, seed=7, cuda_graph=True)
+        b.compile(integrands.symgauss())
+        res, sig = b.run_integration(3)
+        assert np.isfinite(res) and sig > 0
+    finally:
+        gc.set_threshold(*old)
+
+
 def test_graph_grows_history():
     inst = VegasFlow(2, 20_000, verbose=False, seed=3, cuda_graph=True)
     inst.compile(integrands.symgauss())

@@ -32,7 +32,7 @@ def _one_pass(inst, u, train=True):
     inst._sample(n, 0, 0, inst._int_id, inst._params_dev, train, False, u_inj=u)
     inst._end_iteration(train=False, n_events=n, want_hist=True, want_sums=True)
     ws = inst._workspace()
-    flags = int(ws["flags"].item())
+    flags = int(ws["flags"][0].item())
     return ws["sums"].cpu().numpy().copy(), ws["hist"].cpu().numpy().copy(), flags
 
 

@@ -258,7 +258,7 @@ def test_index_range_flag_on_bad_injected_uniforms():
     inst.set_uniform_source(lambda m, d: bad)
     inst.run_integration(1)  # logs the warning, clears the flag
     flags = inst._workspace()["flags"]
-    assert int(flags.item()) == 0
+    assert int(flags[0].item()) == 0
 
 
 def test_abi_rejects_bad_arguments():

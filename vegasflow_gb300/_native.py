@@ -143,6 +143,11 @@ def ptr(t):
 
 
 def stream_handle(stream=None):
+    """cudaStream_t of ``stream`` (default: the current stream of the current device)."""
     import torch
-    s = stream if stream is not None else torch.cuda.current_stream()
-    return ctypes.c_void_p(s.cuda_stream)
+    if stream is not None:
+        return ctypes.c_void_p(stream.cuda_stream)
+    raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+    if raw is not None:  # the same handle without torch.cuda.current_stream()'s Python-side checks
+        return ctypes.c_void_p(raw(torch._C._cuda_getDevice()))
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)

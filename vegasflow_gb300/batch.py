@@ -24,7 +24,7 @@ import torch
 from . import _native as nat
 from .configflow import BINS_MAX
 from .integrands import CudaIntegrand, DeviceIntegrand
-from .utils import preload_kernels
+from .utils import capture_guard, preload_kernels
 
 ITEM_DTYPE = np.dtype([("n_events", "<i8"), ("grid_off", "<i8"), ("param_off", "<i8"), ("xjac", "<f8"),
                        ("n_dim", "<i4"), ("integrand", "<i4"), ("stream_id", "<i4"), ("tile0", "<i4"),
@@ -196,7 +196,7 @@ class VegasBatch:
         side.wait_stream(torch.cuda.current_stream(self.device))
         g = torch.cuda.CUDAGraph()
         # the captured launches must see the counters' device addresses only
-        with torch.cuda.stream(side):
+        with capture_guard(), torch.cuda.stream(side):
             with torch.cuda.graph(g, stream=side):
                 self._launch_iteration()
         torch.cuda.current_stream(self.device).wait_stream(side)

@@ -121,8 +121,9 @@ vf_iteration_end_kernel(const IterEndArgs a) {
       // monte_carlo.py:712-732, accumulated iteration by iteration
       double* av = a.avg + 5 * j;
       const double wgt = 1.0 / __dmul_rn(sigma, sigma);
-      av[0] = __dadd_rn(av[0], __dmul_rn(res, wgt));
-      av[1] = __dadd_rn(av[1], wgt);
+      // history row 0 starts a new average: the buffer's previous contents are not read
+      av[0] = it == 0 ? __dmul_rn(res, wgt) : __dadd_rn(av[0], __dmul_rn(res, wgt));
+      av[1] = it == 0 ? wgt : __dadd_rn(av[1], wgt);
       const double mean = av[0] / av[1];
       av[2] = mean;
       av[3] = sqrt(1.0 / av[1]);

@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "vegasflow_gb300.h"
 #include "vf_internal.h"
@@ -55,6 +58,31 @@ int sm_count() {
   return n;
 }
 
+// Resident blocks per SM of the VEGAS+ sampler that Philox iterations launch for
+// (precision, n_dim) -- in fp32 the float32 kernel, in float64 the generic one --
+// the smallest over the built-in integrands; computed once per configuration.
+int plus_blocks_per_sm(int precision, int n_dim) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(precision, n_dim);
+  const auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int best = 0;
+  for (int integ = VF_INT_SYMGAUSS; integ <= VF_INT_SUM; ++integ) {
+    const bool f32 = precision == VF_PREC_F32;
+    const void* k = f32 ? vf::plus_f32_kernel(n_dim, integ) : plus_kernel(precision, n_dim, integ);
+    const int smem = f32 ? vf::plus_f32_smem_bytes(n_dim, 1) : vf::plus_smem_bytes(8, n_dim, 1);
+    int per_sm = 0;
+    if (k && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, VF_THREADS, smem) == cudaSuccess &&
+        per_sm > 0 && (best == 0 || per_sm < best))
+      best = per_sm;
+  }
+  if (best == 0) best = 1;
+  cache[key] = best;
+  return best;
+}
+
 }  // namespace
 
 extern "C" {
@@ -62,13 +90,14 @@ extern "C" {
 int vf_plus_rows(int precision, int n_dim, int n_hcubes, int* rows) {
   if (!rows || n_dim < 1 || n_dim > VF_MAX_DIM || n_hcubes < 1)
     return err(VF_ERR_ARG, "vf_plus_rows: bad arguments");
+  if (precision != VF_PREC_F64 && precision != VF_PREC_F32) return err(VF_ERR_ARG, "vf_plus_rows: precision");
   const int sms = sm_count();
   if (sms <= 0) return err(VF_ERR_CUDA, "vf_plus_rows: no CUDA device");
-  // one warp per hypercube, at most 4 blocks per SM of 8 warps
+  // one warp per hypercube, at most one wave of resident blocks: a second,
+  // partial wave would hold the iteration for a whole hypercube's time
   int need = (n_hcubes + VF_THREADS / 32 - 1) / (VF_THREADS / 32);
-  const int cap = 4 * sms;
+  const int cap = plus_blocks_per_sm(precision, n_dim) * sms;
   *rows = need < cap ? need : cap;
-  (void)precision;
   return VF_OK;
 }
 

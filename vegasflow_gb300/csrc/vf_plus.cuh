@@ -246,8 +246,9 @@ vf_plus_iteration_end_kernel(const PlusEndArgs a) {
         hrow[0] = res;
         hrow[1] = sigma;
         const double wgt = 1.0 / __dmul_rn(sigma, sigma);
-        a.avg[0] = __dadd_rn(a.avg[0], __dmul_rn(res, wgt));
-        a.avg[1] = __dadd_rn(a.avg[1], wgt);
+        // history row 0 starts a new average: the buffer's previous contents are not read
+        a.avg[0] = it == 0 ? __dmul_rn(res, wgt) : __dadd_rn(a.avg[0], __dmul_rn(res, wgt));
+        a.avg[1] = it == 0 ? wgt : __dadd_rn(a.avg[1], wgt);
         const double mean = a.avg[0] / a.avg[1];
         a.avg[2] = mean;
         a.avg[3] = sqrt(1.0 / a.avg[1]);

@@ -24,7 +24,7 @@ __host__ __device__ inline int plus_f32_smem_bytes(int D, int train, int threads
 }
 
 template <int D, int INTEG>
-__global__ void __launch_bounds__(VF_THREADS) vf_plus_f32_kernel(const PlusArgs a) {
+__global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel(const PlusArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NB = D * VF_BINS;
   float2* cells = reinterpret_cast<float2*>(smem);

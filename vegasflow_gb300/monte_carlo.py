@@ -262,7 +262,9 @@ class MonteCarloFlow(ABC):
         if ws.get("key") != self._width():
             ws.clear()
             ws["key"] = self._width()
-            ws["flags"] = torch.zeros(1, dtype=torch.int32, device=self.device)
+            # the flags word (kernels or VF_FLAG_* bits into element 0) padded to 8 bytes, so
+            # that run_integration reads it as one float64 slot of its single D2H copy
+            ws["flags"] = torch.zeros(2, dtype=torch.int32, device=self.device)
             ws["history"] = torch.zeros((16, 2 * self._n_out), dtype=torch.float64, device=self.device)
             ws["avg"] = torch.zeros(5 * self._n_out, dtype=torch.float64, device=self.device)
             ws["hist"] = torch.zeros((self.n_dim, BINS_MAX), dtype=torch.float64, device=self.device)
@@ -282,9 +284,11 @@ class MonteCarloFlow(ABC):
             ws["history"] = grow
         return ws
 
-    def _reset_average(self):
-        ws = self._workspace()
-        ws["avg"].zero_()
+    def _reset_average(self, clear=False):
+        """Start a new weighted average: history row 0 makes the iteration-end
+        kernels overwrite the average, so the buffer is only cleared on request."""
+        if clear:
+            self._workspace()["avg"].zero_()
         self._it = 0
 
     # ---------------------------------------------------------------- sampling
@@ -586,13 +590,13 @@ class MonteCarloFlow(ABC):
         self._apply_shape()
         key = self._graph_signature(ws)
         if self._graph is None or self._graph_key != key:
-            from .utils import preload_kernels
+            from .utils import capture_guard, preload_kernels
             preload_kernels(self.device)
             torch.cuda.synchronize(self.device)
             side = torch.cuda.Stream(device=self.device)
             side.wait_stream(torch.cuda.current_stream(self.device))
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.stream(side):
+            with capture_guard(), torch.cuda.stream(side):
                 with torch.cuda.graph(g, stream=side):
                     self._graph_call(ws)
             torch.cuda.current_stream(self.device).wait_stream(side)
@@ -624,7 +628,7 @@ class MonteCarloFlow(ABC):
         VegasFlowPlus) the iterations are replays of one captured CUDA graph (two
         kernels, no host work between iterations)."""
         self._require_gpu()
-        self._reset_average()
+        self._reset_average(clear=n_iter < 1)
         first = len(self._history)
         all_results = []
         graph = self._graph_ready(histograms)
@@ -652,12 +656,14 @@ class MonteCarloFlow(ABC):
                     info = [print_iteration(i, float(res), float(error), extra=time_str)]
                 logger.info("\n      ".join(info))
         ws = self._workspace()
+        # one copy of history rows, average and the flags word (its bits carried
+        # through a float64 slot, which the copies move without arithmetic)
         host = torch.cat([ws["history"][: self._it].reshape(-1), ws["avg"],
-                          ws["flags"].to(torch.float64)]).cpu().numpy()
+                          ws["flags"].view(torch.float64)]).cpu().numpy()
         k = self._n_out
         hist_rows = host[: self._it * 2 * k].reshape(self._it, 2 * k)
         avg = host[self._it * 2 * k: self._it * 2 * k + 5 * k].reshape(k, 5)
-        flags = int(host[-1])
+        flags = int(host[-1:].view(np.int32)[0])
         self._check_flags(flags)
         base = self._it - n_iter
         for i in range(n_iter):

@@ -2,6 +2,9 @@
 
 from __future__ import annotations
 
+import contextlib
+import gc
+
 import torch
 
 from . import _native as nat
@@ -31,6 +34,22 @@ def py_consume_array_into_indices(input_arr, indices, result_size):
 
 
 _PRELOADED = set()
+
+
+@contextlib.contextmanager
+def capture_guard():
+    """Around a CUDA-graph capture: collect Python's cyclic garbage first and
+    keep the collector off until the capture ends.  A collection inside the
+    capture could run the finalizer of an unreachable CUDA graph, whose reset
+    is not permitted while a stream captures and invalidates the capture."""
+    gc.collect()
+    enabled = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if enabled:
+            gc.enable()
 
 
 def preload_kernels(device):
