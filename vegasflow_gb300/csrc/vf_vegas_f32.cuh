@@ -341,6 +341,23 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
       if (have) add_fixed(bins, v2, ev);
       e += stride;
     }
+    // Two events per pass give the scheduler two independent draws to overlap
+    // (shared-memory latency of one with the Philox rounds of the other).
+    // Measured (1e8 events): faster for D <= 4 (0.560 vs 0.582 ms training)
+    // and for frozen grids (D = 8: 0.764 vs 0.799 ms), slower when training at
+    // D >= 8 (D = 8: 0.989 vs 0.975 ms), where the histogram atomics dominate.
+    if (!fixedp && (D <= 4 || !train)) {
+      for (; e + stride < n; e += 2 * stride) {
+        const u64 ev0 = (u64)(a.ev_offset + e), ev1 = ev0 + (u64)stride;
+        int b0[D], b1[D];
+        float x0[D], x1[D];
+        float wf0 = 1.0f, s0 = 0.0f, wf1 = 1.0f, s1_ = 0.0f;
+        draw(ev0, b0, wf0, s0, x0);
+        draw(ev1, b1, wf1, s1_, x1);
+        finish(b0, wf0, s0, x0);
+        finish(b1, wf1, s1_, x1);
+      }
+    }
     for (; e < n; e += stride) {
       const u64 ev = (u64)(a.ev_offset + e);
       int bins[D];
