@@ -59,26 +59,27 @@ __host__ __device__ inline int vegas_f32_joint_floats(int D) { return (D / 2) * 
 // The reference's bin of an injected float64 uniform u, ind = trunc(fl(50 *
 // fl(1 - u))) (vflow.py:117, :67), without float64 arithmetic: for u in
 // [2^-12, 1), U = u 2^64 is an exact 64-bit integer and y = 50 (1 - u) is
-// exactly (50 (2^64 - U)) / 2^64, an integer part and a 64-bit fraction.  The
-// reference's two roundings move y by less than 100 2^-53 < 2^-46, so
-// trunc(xn) = trunc(y) unless the fraction's top 32 bits are all zeros or all
-// ones (y within 2^-32 of an integer), where the caller repeats the float64
-// operations; so does every u outside [2^-12, 1) (and NaN, negative, >= 1).
-// m = 1 + the fraction's top 23 bits.  32-bit operations throughout: about 14
-// per uniform.  Returns false for the float64 cases.
+// exactly 50 (2^64 - U) / 2^64.  With h = the high word of U, P = 50 (2^32 - 1 - h)
+// is a 38-bit integer and y 2^32 = P + c, c in [0, 50] (c holds the low word's
+// share).  So when the low 32 bits f of P lie in [1, 2^32 - 52], adding c neither
+// carries into the integer part nor lands within 2^-32 of an integer: ind = P >> 32
+// is trunc(y), and the reference's two roundings (which move y by less than
+// 100 2^-53 < 2^-46) cannot change it.  Otherwise (f within 52 of an integer
+// boundary, about 1 uniform in 8e7) -- and for every u outside [2^-12, 1), NaN,
+// negative, >= 1 -- the caller repeats the float64 operations.  m = 1 + f's top
+// 23 bits (below 1 + the true fraction by less than 2^-23 + 51 2^-32).  About 10
+// 32-bit operations per uniform.  Returns false for the float64 cases.
 __device__ __forceinline__ bool inj_bin_exact(u64 bits, int& ind, float& m) {
   const u32 bh = (u32)(bits >> 32), bl = (u32)bits;
   const u32 sh = (bh >> 20) - 1011u;  // biased exponent - 1011: u in [2^-12, 1) <=> sh in [0, 11]
   if (sh > 11u) return false;
   const u32 mh = (bh & 0xFFFFFu) | 0x100000u;  // the mantissa's high word, implicit bit set
-  const u64 uu = ((u64)__funnelshift_l(bl, mh, sh) << 32) | (u64)(bl << sh);  // U = mantissa << sh
-  const u64 v = 0ull - uu;                                                      // 2^64 - U
-  const u64 p0 = (u64)(u32)v * 50ull;
-  const u64 p1 = (u64)(u32)(v >> 32) * 50ull + (p0 >> 32);  // 50 v = p1 2^32 + (u32)p0
-  const u32 fh = (u32)p1;                                    // the fraction's top 32 bits
-  if (fh + 1u < 2u) return false;
-  ind = (int)(p1 >> 32);
-  m = __uint_as_float((fh >> 9) | 0x3F800000u);
+  const u32 h = __funnelshift_l(bl, mh, sh);   // high word of U = mantissa << sh
+  const u64 P = (u64)(~h) * 50ull;
+  const u32 f = (u32)P;
+  if (f - 1u >= 0xFFFFFFCCu) return false;  // f outside [1, 2^32 - 52]
+  ind = (int)(P >> 32);
+  m = __uint_as_float(__funnelshift_r(f, 0x7Fu, 9));  // 0x3F800000 | (f >> 9)
   return true;
 }
 
