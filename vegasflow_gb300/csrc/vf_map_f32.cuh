@@ -5,13 +5,15 @@
 // one FMA through the staged per-bin table -- and the event's x (D floats),
 // weight w (float) and, when asked, bin indices (D int32) go to HBM.
 //
-// The stores are the whole cost (36 bytes per event at D = 8 for x and w), so
-// they are staged: each thread writes its events' rows into a shared-memory
-// tile of VF_MAP_EPT x THREADS events, and one thread hands each full tile to the bulk-copy
-// engine (cp.async.bulk shared -> global, contiguous, 16-byte aligned), two
-// tiles in flight.  A thread's own row stores would cost a warp 32 separate
-// 32-byte segments per dimension; a tile is one contiguous transfer.  The last
-// partial tile, and arrays that are not 16-byte aligned, use plain stores.
+// The stores are most of the cost (36 bytes per event at D = 8 for x and w), so
+// they are staged: each warp writes its lanes' rows into its own shared-memory
+// tile of VF_MAP_EPT x 32 events, and lane 0 hands each full tile to the
+// bulk-copy engine (cp.async.bulk shared -> global, contiguous, 16-byte
+// aligned), two tiles per warp in flight, with no block-wide barrier (measured
+// 2 % faster than block tiles behind __syncthreads).  A thread's own row stores
+// would cost a warp 32 separate 32-byte segments per dimension; a tile is one
+// contiguous transfer.  The last partial tile, and arrays that are not 16-byte
+// aligned, use plain stores.
 #pragma once
 #include "vf_vegas_f32.cuh"
 
@@ -90,33 +92,37 @@ vf_vegas_f32_map_kernel(const __grid_constant__ SampleArgs a) {
   __syncthreads();
   const float wscale = g_wscale;
 
-  // ---- staging tiles of T = VF_MAP_EPT * THREADS events:
-  // [x: T*D floats][ind: T*D ints][w: T floats], two of them
+  // ---- staging: per warp two tiles of WT = VF_MAP_EPT * 32 events, each
+  // [x: WT*D floats][ind: WT*D ints][w: WT floats]
   const bool want_ind = ind_out != nullptr;
-  constexpr int T = VF_MAP_EPT * THREADS;
-  constexpr u32 XB = T * D * 4, WB = T * 4;
-  const u32 stage_bytes = XB * (want_ind ? 2u : 1u) + WB;
   unsigned char* stage0 = smem + ((NB * 8 + 15) & ~15);
   const bool aligned = ((reinterpret_cast<size_t>(x_out) | reinterpret_cast<size_t>(w_out) |
                          reinterpret_cast<size_t>(ind_out)) & 15) == 0;
   const long long n = a.n_events;
-  const long long n_tiles = (n + T - 1) / T;
+  // a warp hands its own tiles to the copy engine: no block-wide barrier
+  const int lane = tid & 31, warp = tid >> 5;
+  constexpr int WT = VF_MAP_EPT * 32;
+  constexpr u32 XBW = WT * D * 4, WBW = WT * 4;
+  const u32 wstage = XBW * (want_ind ? 2u : 1u) + WBW;
+  unsigned char* wbase = stage0 + (size_t)warp * 2 * wstage;
+  const long long n_wt = (n + WT - 1) / WT;
   int it = 0;
-  for (long long t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
-    const long long e0 = t * T;
-    const bool full = aligned && e0 + T <= n;
-    unsigned char* st = stage0 + (it & 1) * stage_bytes;
+  for (long long t = (long long)blockIdx.x * (THREADS / 32) + warp; t < n_wt;
+       t += (long long)gridDim.x * (THREADS / 32), ++it) {
+    const long long e0 = t * WT;
+    const bool full = aligned && e0 + WT <= n;  // warp-uniform
+    unsigned char* st = wbase + (it & 1) * wstage;
     u32* xs = reinterpret_cast<u32*>(st);
-    u32* is = reinterpret_cast<u32*>(st + XB);
-    float* wsm = reinterpret_cast<float*>(st + XB * (want_ind ? 2 : 1));
+    u32* is = reinterpret_cast<u32*>(st + XBW);
+    float* wsm = reinterpret_cast<float*>(st + XBW * (want_ind ? 2 : 1));
     if (full) {
       // the stage's previous tile (two tiles back) must have been read out
-      if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-      __syncthreads();
+      if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+      __syncwarp();
     }
 #pragma unroll
     for (int k = 0; k < VF_MAP_EPT; ++k) {
-      const int r = k * THREADS + tid;  // row in the tile
+      const int r = k * 32 + lane;  // row in the warp's tile
       const long long e = e0 + r;
       if (e < n) {
         const u64 ev = (u64)(a.ev_offset + e);
@@ -160,16 +166,16 @@ vf_vegas_f32_map_kernel(const __grid_constant__ SampleArgs a) {
     }
     if (full) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the rows, to the copy engine
-      __syncthreads();
-      if (tid == 0) {
-        if (x_out) bulk_store(x_out + e0 * D, smem_u32(xs), XB);
-        if (want_ind) bulk_store(ind_out + e0 * D, smem_u32(is), XB);
-        if (w_out) bulk_store(w_out + e0, smem_u32(wsm), WB);
+      __syncwarp();
+      if (lane == 0) {
+        if (x_out) bulk_store(x_out + e0 * D, smem_u32(xs), XBW);
+        if (want_ind) bulk_store(ind_out + e0 * D, smem_u32(is), XBW);
+        if (w_out) bulk_store(w_out + e0, smem_u32(wsm), WBW);
         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
       }
     }
   }
-  if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 }  // namespace vf
