@@ -181,3 +181,24 @@ def test_cuda_integrand_compiles_without_gpu():
     bad = integrands.cuda_integrand("__device__ vf_real bad(const vf_real* x) { return y; }", "bad")
     ok, log = bad.check()
     assert not ok and "undefined" in log
+
+
+def test_generate_condition_function():
+    """test_utils.py:40-70: 'and', 'or', a list of conditions, and the errors."""
+    from vegasflow_gb300.utils import generate_condition_function
+
+    rng = np.random.default_rng(2)
+    np_masks = rng.integers(2, size=(4, 15)).astype(bool)
+    masks = [torch.as_tensor(m) for m in np_masks]
+
+    def check(np_mask, mask, idx):
+        np.testing.assert_array_equal(np_mask, mask.numpy())
+        np.testing.assert_array_equal(np.array(np_mask.nonzero()).T, idx.numpy())
+        assert idx.dtype == torch.int32
+
+    check(np.all(np_masks, axis=0), *generate_condition_function(4, "and")(*masks))
+    check(np.any(np_masks, axis=0), *generate_condition_function(4, "or")(*masks))
+    check(np_masks[0] & np_masks[1] | np_masks[2], *generate_condition_function(3, ["and", "or"])(*masks[:3]))
+    for args in ((1, "and"), (5, "bad_condition"), (5, ["or", "and"]), (3, ["or", "bad_condition"])):
+        with pytest.raises(ValueError):
+            generate_condition_function(*args)

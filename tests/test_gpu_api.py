@@ -253,3 +253,28 @@ def test_user_histograms():
     assert abs(h.sum() - res) < 1e-6 * abs(res)
     np.testing.assert_allclose(h, [res / 2, res / 2], atol=5 * sigma)
     assert len(inst.history) == 5 and all(len(e[2]) == 1 for e in inst.history)
+
+
+@pytest.mark.parametrize("kind", ["device", "torch"])
+def test_run_event_and_device_run(kind):
+    """run_event: one iteration's (res, res2, arr_res2) with the grid and the average
+    untouched (monte_carlo.py:420-480); device_run(ncalls): the same for the first
+    ncalls events, weighted as part of the n_events iteration, on the device taken
+    from (and handed back to) the pool (monte_carlo.py:318-365)."""
+    n = 200_000
+    inst = VegasFlow(3, n, verbose=False, seed=4)
+    inst.compile(integrands.symgauss() if kind == "device" else example_integrand)
+    inst.run_integration(2)
+    grid0 = inst.divisions.clone()
+    res, res2, hist = inst.run_event()
+    assert torch.equal(inst.divisions, grid0)
+    assert tuple(hist.shape) == (3, 50) and float(hist.sum()) > 0
+    sig = float(np.sqrt(max((n * float(res2) - float(res) ** 2) / (n - 1), 0.0)))
+    assert abs(float(res) - 1.0) < 5 * sig
+    half = inst.device_run(n // 2)
+    assert len(half) == 3 and abs(float(half[0]) - 0.5) < 5 * sig
+    assert inst.device_run(n, sent_pc=50.0)[0].shape == res.shape
+    dev = inst.get_device()
+    assert dev == inst.device and inst.get_device() is None
+    inst.release_device(dev)
+    assert inst.get_device() == dev

@@ -29,6 +29,7 @@ import copy
 import inspect
 import logging
 import os
+import threading
 import time
 from abc import ABC, abstractmethod
 
@@ -124,7 +125,8 @@ class MonteCarloFlow(ABC):
         self.distribute = False
         self._pass_weight = False
         self.list_devices = list_devices
-        self.devices = None
+        self.devices = None  # the device pool (get_device / release_device): this integrator's GPU
+        self.lock = threading.Lock()
         self.precision = (precision or DEFAULT_PRECISION).lower()
         if self.precision not in ("fp64", "fp32"):
             raise ValueError(f"precision must be 'fp64' or 'fp32', not {precision!r}")
@@ -311,15 +313,16 @@ class MonteCarloFlow(ABC):
             raise ValueError(f"uniform source returned shape {tuple(u.shape)}, expected {(n, self.n_dim)}")
         return u
 
-    def _fill_partials(self, train):
-        """All events of one iteration into the block-partial rows."""
+    def _fill_partials(self, train, n_events=None):
+        """All events of one iteration (or the first ``n_events`` of one, weighted
+        as part of the whole iteration) into the block-partial rows."""
         self._require_gpu()
         if self.event is None:
             raise RuntimeError("Compile must be ran before running any iterations")
         call = self._next_call()
+        n = self.n_events if n_events is None else int(n_events)
         if self._kind == "device":
             self._apply_shape()
-            n = self.n_events
             if self._uniform_source is None:
                 self._sample(n, 0, call, self._int_id, self._params_dev, train, False)
             else:
@@ -330,7 +333,7 @@ class MonteCarloFlow(ABC):
                     off += nc
         else:
             off = 0
-            for i, nc in enumerate(_chunk_sizes(self.n_events, self.events_per_run)):
+            for i, nc in enumerate(_chunk_sizes(n, self.events_per_run)):
                 self._torch_chunk(nc, off, call, train, accumulate=i > 0)
                 off += nc
 
@@ -381,8 +384,13 @@ class MonteCarloFlow(ABC):
         arr_res2]) as device tensors (monte_carlo.py:420-480)."""
         if self._differentiable and self._kind == "torch":
             return self._run_event_autograd()
+        return self._event_sums(self.n_events)
+
+    def _event_sums(self, n_events):
+        """(res, res2[, arr_res2]) of ``n_events`` events of an iteration, without
+        touching the grid or the running average."""
         want_hist = self._ALG == nat.VF_ALG_VEGAS and self._train_now()
-        self._fill_partials(train=want_hist)
+        self._fill_partials(train=want_hist, n_events=n_events)
         ws = self._history_slot()
         saved = self._it
         # a scratch history slot so the running average is left untouched
@@ -756,6 +764,42 @@ class MonteCarloFlow(ABC):
         if want_hist:
             return res, res2, hist
         return res, res2
+
+    # ---------------------------------------------------------------- device pool
+    def get_device(self):
+        """The first free device of the pool, now taken, or None (monte_carlo.py:318-332);
+        the pool is this integrator's GPU."""
+        with self.lock:
+            if self.devices is None:
+                self.devices = {self.device: True}
+            for device, available in self.devices.items():
+                if available:
+                    self.devices[device] = False
+                    return device
+        return None
+
+    def release_device(self, device):
+        """Makes ``device`` available again (monte_carlo.py:334-340)."""
+        with self.lock:
+            if self.devices is None:
+                self.devices = {}
+            self.devices[device] = True
+
+    def device_run(self, ncalls, sent_pc=100.0, **kwargs):
+        """The accumulables (res, res2[, arr_res2]) of ``ncalls`` events, weighted as
+        part of an ``n_events`` iteration, on the pool's device (monte_carlo.py:342-365)."""
+        if self._verbose:
+            print(f"Events sent to the computing device: {sent_pc:.1f} %", end="\r")
+        if not self.event:
+            raise RuntimeError("Compile must be ran before running any iterations")
+        device = self.get_device()
+        try:
+            if self._differentiable and self._kind == "torch" and int(ncalls) == self.n_events:
+                return self._run_event_autograd()
+            return self._event_sums(int(ncalls))
+        finally:
+            if device is not None:
+                self.release_device(device)
 
     def set_distribute(self, queue_object):
         raise NotImplementedError("dask distribution is not part of the GB300 build (one GPU)")

@@ -1,4 +1,6 @@
-"""Utilities (vegasflow utils.py): the per-bin histogram."""
+"""Utilities (vegasflow utils.py): the per-bin histogram, the mask combiner for
+integrands, and the GPU-side helpers of this package (kernel preloading, the
+capture guard)."""
 
 from __future__ import annotations
 
@@ -31,6 +33,42 @@ def consume_array_into_indices(input_arr, indices, result_size):
 def py_consume_array_into_indices(input_arr, indices, result_size):
     """Python-object interface of ``consume_array_into_indices`` (utils.py:47-52)."""
     return consume_array_into_indices(input_arr, indices, int(result_size))
+
+
+def generate_condition_function(n_mask, condition="and"):
+    """A function ``f(*masks) -> (mask, indices)`` combining ``n_mask`` boolean
+    tensors with ``condition`` ("and", "or", or a list of n_mask - 1 of them
+    applied left to right); ``indices`` are the positions where the combined mask
+    is True, int32 of shape (k, 1) (utils.py:55-141, same errors)."""
+    allowed = {"and": torch.logical_and, "or": torch.logical_or}
+    names = list(allowed)
+    if n_mask < 2:
+        raise ValueError("At least two masks needed to generate a wrapper")
+    if isinstance(condition, str):
+        if condition not in allowed:
+            raise ValueError(f"Wrong condition {condition}, allowed values are {names}")
+        conditions = None
+    else:
+        conditions = list(condition)
+        if len(conditions) != n_mask - 1:
+            raise ValueError(f"Wrong number of conditions for {n_mask} masks: {len(conditions)}")
+        for cond in conditions:
+            if cond not in allowed:
+                raise ValueError(f"Wrong condition {cond}, allowed values are {names}")
+
+    def condition_to_idx(*masks):
+        masks = [torch.as_tensor(m, dtype=torch.bool) for m in masks]
+        if conditions is not None:
+            res = masks[0]
+            for cond, mask in zip(conditions, masks[1:]):
+                res = allowed[cond](res, mask)
+        elif condition == "and":
+            res = torch.stack(masks).all(dim=0)
+        else:
+            res = torch.stack(masks).any(dim=0)
+        return res, torch.nonzero(res).to(torch.int32)
+
+    return condition_to_idx
 
 
 _PRELOADED = set()

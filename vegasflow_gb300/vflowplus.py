@@ -280,6 +280,14 @@ class VegasFlowPlus(VegasFlow):
             return out + (ws["hist"].clone(),)
         return out
 
+    def _event_sums(self, n_events):
+        # the hypercube allocation covers whole iterations (events_limit = n_events,
+        # vflowplus.py:88-100), so a device run is always one
+        if int(n_events) != self.n_events:
+            raise NotImplementedError(f"VegasFlowPlus runs whole iterations of {self.n_events} events, "
+                                      f"not {n_events}")
+        return self.run_event()
+
     def _generate_random_array(self, n_events, *args):
         """(x, w, ind, segm) of one full iteration's layout (vflowplus.py:165-171)."""
         self._require_gpu()
