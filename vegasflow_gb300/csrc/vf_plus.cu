@@ -58,6 +58,24 @@ int sm_count() {
   return n;
 }
 
+// Raise a VEGAS+ sampler's dynamic shared-memory limit once per (device, kernel)
+// and size (launches inside a stream capture then make no attribute calls).
+int plus_prepare_smem(const void* k, int smem) {
+  if (smem <= 48 * 1024) return VF_OK;
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(dev, k);
+  const auto it = done.find(key);
+  if (it != done.end() && it->second >= smem) return VF_OK;
+  const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return err(VF_ERR_CUDA, cudaGetErrorString(e));
+  done[key] = smem;
+  return VF_OK;
+}
+
 // Resident blocks per SM of the VEGAS+ sampler that Philox iterations launch for
 // (precision, n_dim) -- in fp32 the float32 kernel, in float64 the generic one --
 // the smallest over the built-in integrands; computed once per configuration.
@@ -74,7 +92,8 @@ int plus_blocks_per_sm(int precision, int n_dim) {
     const void* k = f32 ? vf::plus_f32_kernel(n_dim, integ) : plus_kernel(precision, n_dim, integ);
     const int smem = f32 ? vf::plus_f32_smem_bytes(n_dim, 1) : vf::plus_smem_bytes(8, n_dim, 1);
     int per_sm = 0;
-    if (k && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, VF_THREADS, smem) == cudaSuccess &&
+    if (k && plus_prepare_smem(k, smem) == VF_OK &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, VF_THREADS, smem) == cudaSuccess &&
         per_sm > 0 && (best == 0 || per_sm < best))
       best = per_sm;
   }
@@ -166,6 +185,8 @@ int plus_sample_impl(int precision, const double* grid, int n_dim, int n_strat, 
   }
   const int smem = f32 ? vf::plus_f32_smem_bytes(n_dim, a.train)
                        : vf::plus_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, a.train);
+  const int rs = plus_prepare_smem(k, smem);
+  if (rs != VF_OK) return rs;
   void* args[] = {&a};
   const cudaError_t e = cudaLaunchKernel(k, dim3(rows), dim3(VF_THREADS), args, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return err(VF_ERR_LAUNCH, cudaGetErrorString(e));

@@ -13,14 +13,20 @@
 // rounded once from float64, integration limits folded), the weight
 // prod(c1) 50^D xjac / n_ev, the integrand in float32, per-hypercube sums with
 // TwoSum-compensated float32 warp reductions written as float64, and the
-// (w f)^2 histogram in per-warp shared tables.
+// (w f)^2 histogram in shared tables, VF_PLUS_HIST_COPIES per warp.
 #pragma once
 #include "vf_plus_args.cuh"
 
 namespace vf {
 
+// Histogram copies per warp, one per group of 32 / VF_PLUS_HIST_COPIES lanes.  The
+// lanes of a warp sample one hypercube, whose events fall in the same ~50 / n_strat
+// bins of every dimension, so one table per warp makes the float atomics (compare-
+// and-swap loops) of a warp instruction collide on a handful of addresses.
+#define VF_PLUS_HIST_COPIES 4
+
 __host__ __device__ inline int plus_f32_smem_bytes(int D, int train, int threads = VF_THREADS) {
-  return D * VF_BINS * 8 + (train ? (threads / 32) * D * VF_BINS * 4 : 0);
+  return D * VF_BINS * 8 + (train ? (threads / 32) * VF_PLUS_HIST_COPIES * D * VF_BINS * 4 : 0);
 }
 
 template <int D, int INTEG>
@@ -43,8 +49,9 @@ __global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel
     }
     cells[k] = make_float2((float)c0, (float)c1);
   }
+  constexpr int NCOPIES = (VF_THREADS / 32) * VF_PLUS_HIST_COPIES;
   if (train)
-    for (int k = tid; k < (VF_THREADS / 32) * NB; k += blockDim.x) hist[k] = 0.0f;
+    for (int k = tid; k < NCOPIES * NB; k += blockDim.x) hist[k] = 0.0f;
   __shared__ float s_wscale;
   if (tid == 0) {
     double ws = a.xjac;  // 1 / n_hcubes (vflowplus.py:144-146)
@@ -55,7 +62,7 @@ __global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel
   const float wscale = s_wscale;
   IntegrandConsts<float, D> kc;
   load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
-  float* my_hist = hist + warp * NB;
+  float* my_hist = hist + (warp * VF_PLUS_HIST_COPIES + lane / (32 / VF_PLUS_HIST_COPIES)) * NB;
   u32 cw2, cw3;
   plus_call_words(a, cw2, cw3);
   const u32 ns = (u32)a.n_strat;
@@ -152,7 +159,7 @@ __global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel
   if (train)
     for (int k = tid; k < NB; k += blockDim.x) {
       float hf = 0.0f;
-      for (int c = 0; c < VF_THREADS / 32; ++c) hf += hist[c * NB + k];
+      for (int c = 0; c < NCOPIES; ++c) hf += hist[c * NB + k];
       row[2 + k] = (double)hf;
     }
 }
