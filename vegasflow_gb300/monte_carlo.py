@@ -264,11 +264,7 @@ class MonteCarloFlow(ABC):
         if ws.get("key") != self._width():
             ws.clear()
             ws["key"] = self._width()
-            # the flags word (kernels or VF_FLAG_* bits into element 0) padded to 8 bytes, so
-            # that run_integration reads it as one float64 slot of its single D2H copy
-            ws["flags"] = torch.zeros(2, dtype=torch.int32, device=self.device)
-            ws["history"] = torch.zeros((16, 2 * self._n_out), dtype=torch.float64, device=self.device)
-            ws["avg"] = torch.zeros(5 * self._n_out, dtype=torch.float64, device=self.device)
+            self._state_rows(ws, 16)
             ws["hist"] = torch.zeros((self.n_dim, BINS_MAX), dtype=torch.float64, device=self.device)
             ws["sums"] = torch.zeros(2 * self._n_out, dtype=torch.float64, device=self.device)
         if ws.get("rows") != self._rows:  # the launch shape sets the partial-row count
@@ -277,13 +273,25 @@ class MonteCarloFlow(ABC):
                                          device=self.device)
         return ws
 
+    def _state_rows(self, ws, rows):
+        """One float64 device buffer [avg (5 n_out) | flags (2 int32) | history (rows x
+        2 n_out)], so that run_integration reads average, flags and the new history rows
+        with one copy; ws["avg"], ws["flags"] (element 0 takes the VF_FLAG_* bits) and
+        ws["history"] are views of it.  Growing it keeps the contents."""
+        k = self._n_out
+        state = torch.zeros(5 * k + 1 + rows * 2 * k, dtype=torch.float64, device=self.device)
+        old = ws.get("state")
+        if old is not None:
+            state[: old.numel()] = old
+        ws["state"] = state
+        ws["avg"] = state[: 5 * k]
+        ws["flags"] = state[5 * k: 5 * k + 1].view(torch.int32)
+        ws["history"] = state[5 * k + 1:].view(rows, 2 * k)
+
     def _history_slot(self):
         ws = self._workspace()
         if self._it >= ws["history"].shape[0]:
-            grow = torch.zeros((2 * ws["history"].shape[0], 2 * self._n_out), dtype=torch.float64,
-                               device=self.device)
-            grow[: ws["history"].shape[0]] = ws["history"]
-            ws["history"] = grow
+            self._state_rows(ws, 2 * ws["history"].shape[0])
         return ws
 
     def _reset_average(self, clear=False):
@@ -591,8 +599,7 @@ class MonteCarloFlow(ABC):
         of the captured call changed), with room for ``n_iter`` history rows."""
         ws = self._workspace()
         if ws["history"].shape[0] < n_iter:
-            ws["history"] = torch.zeros((max(n_iter, 2 * ws["history"].shape[0]), 2 * self._n_out),
-                                        dtype=torch.float64, device=self.device)
+            self._state_rows(ws, max(n_iter, 2 * ws["history"].shape[0]))
         if "counters" not in ws:
             ws["counters"] = torch.zeros(2, dtype=torch.int32, device=self.device)
         self._apply_shape()
@@ -615,8 +622,11 @@ class MonteCarloFlow(ABC):
         """``n_iter`` iterations as replays of one captured iteration: the Philox
         call counter and the history row advance on the device."""
         g, ws = self._graph_for(n_iter)
+        # the start counters as two device fills: asynchronous, and no pinned host
+        # buffer (whose release could record events on a stream while another captures)
         start = np.array([self._call_ctr & 0xFFFFFFFF, self._it], dtype=np.uint32).view(np.int32)
-        ws["counters"].copy_(torch.from_numpy(start))
+        ws["counters"][0:1].fill_(int(start[0]))
+        ws["counters"][1:2].fill_(int(start[1]))
         for i in range(n_iter):
             if log_time:
                 t0 = time.time()
@@ -664,14 +674,13 @@ class MonteCarloFlow(ABC):
                     info = [print_iteration(i, float(res), float(error), extra=time_str)]
                 logger.info("\n      ".join(info))
         ws = self._workspace()
-        # one copy of history rows, average and the flags word (its bits carried
-        # through a float64 slot, which the copies move without arithmetic)
-        host = torch.cat([ws["history"][: self._it].reshape(-1), ws["avg"],
-                          ws["flags"].view(torch.float64)]).cpu().numpy()
+        # one copy of average, flags word (its bits carried through a float64 slot,
+        # which the copy moves without arithmetic) and history rows
         k = self._n_out
-        hist_rows = host[: self._it * 2 * k].reshape(self._it, 2 * k)
-        avg = host[self._it * 2 * k: self._it * 2 * k + 5 * k].reshape(k, 5)
-        flags = int(host[-1:].view(np.int32)[0])
+        host = ws["state"][: 5 * k + 1 + self._it * 2 * k].cpu().numpy()
+        avg = host[: 5 * k].reshape(k, 5)
+        flags = int(host[5 * k: 5 * k + 1].view(np.int32)[0])
+        hist_rows = host[5 * k + 1:].reshape(self._it, 2 * k)
         self._check_flags(flags)
         base = self._it - n_iter
         for i in range(n_iter):
