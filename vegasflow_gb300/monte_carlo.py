@@ -622,11 +622,11 @@ class MonteCarloFlow(ABC):
         """``n_iter`` iterations as replays of one captured iteration: the Philox
         call counter and the history row advance on the device."""
         g, ws = self._graph_for(n_iter)
-        # the start counters as two device fills: asynchronous, and no pinned host
-        # buffer (whose release could record events on a stream while another captures)
-        start = np.array([self._call_ctr & 0xFFFFFFFF, self._it], dtype=np.uint32).view(np.int32)
-        ws["counters"][0:1].fill_(int(start[0]))
-        ws["counters"][1:2].fill_(int(start[1]))
+        # the start counters (call, iteration) as one 64-bit device fill: asynchronous,
+        # and no pinned host buffer (whose release could record events on a stream
+        # while another stream captures)
+        start = np.array([self._call_ctr & 0xFFFFFFFF, self._it], dtype=np.uint32).view(np.int64)
+        ws["counters"].view(torch.int64).fill_(int(start[0]))
         for i in range(n_iter):
             if log_time:
                 t0 = time.time()
