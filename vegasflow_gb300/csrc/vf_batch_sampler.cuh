@@ -143,7 +143,7 @@ __device__ void batch_tile(const BatchArgs& a, const BatchItem& it, int tile, bo
         if (d < D) {
           const u64 pp = (u64)(~wq[jj]) * 50ull + 25ull;
           const int i = (int)(pp >> 32);
-          const float m = __uint_as_float(__funnelshift_r((u32)pp, 0x7Fu, 9));  // 0x3F800000 | (low word >> 9)
+          const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
           const float2 c = cells[d * VF_BINS + i];
           const float t = fmaf(c.y, m, c.x);
           wf = (d == 0) ? c.y : wf * c.y;

@@ -204,7 +204,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
   // float64 constant of the weight (host-computed): 50^D * xjac, times
   // pref / prod k for the Gaussian family
   const double wscale = g_wscale;
-  const float wscale_f = (float)wscale;  // the full weight handed to a user integrand
+  [[maybe_unused]] const float wscale_f = (float)wscale;  // the full weight handed to a user integrand
   IntegrandConsts<float, D> kc;
   if (!GAUSS) load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
 
@@ -279,7 +279,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
         if (d < D) {
           const u64 pp = (u64)(~wq[j]) * 50ull + 25ull;
           const int i = (int)(pp >> 32);
-          const float m = __uint_as_float(__funnelshift_r((u32)pp, 0x7Fu, 9));  // 0x3F800000 | (low word >> 9)
+          const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
           const float2 c = cells[d * VF_BINS + i];
           const float t = fmaf(c.y, m, c.x);
           wf = (d == 0) ? c.y : wf * c.y;
@@ -344,10 +344,12 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
     }
     // Two events per pass give the scheduler two independent draws to overlap
     // (shared-memory latency of one with the Philox rounds of the other).
-    // Measured (1e8 events): faster for D <= 4 (0.560 vs 0.582 ms training)
-    // and for frozen grids (D = 8: 0.764 vs 0.799 ms), slower when training at
-    // D >= 8 (D = 8: 0.989 vs 0.975 ms), where the histogram atomics dominate.
-    if (!fixedp && (D <= 4 || !train)) {
+    // Measured (1e8 events): faster for D <= 4 (0.560 vs 0.582 ms training,
+    // 0.441 vs 0.490 frozen).  For D >= 5 it made frozen grids faster too (D = 8:
+    // 0.717 vs 0.799 ms) but training slower (D = 8: 0.984 vs 0.975 ms, the
+    // histogram atomics dominate), and the registers it needs slow the training
+    // loop even where it is not taken, so it is compiled for D <= 4 only.
+    if constexpr (D <= 4) if (!fixedp) {
       for (; e + stride < n; e += 2 * stride) {
         const u64 ev0 = (u64)(a.ev_offset + e), ev1 = ev0 + (u64)stride;
         int b0[D], b1[D];
