@@ -14,7 +14,10 @@ class PlainFlow(MonteCarloFlow):
     _GRAPH_ITERATIONS = True
 
     def _run_event(self, integrand, ncalls=None):
-        return self.run_event()
+        """res, res2 of one chunk of ``ncalls`` events (plain.py:18-35)."""
+        if ncalls is None or int(ncalls) == self.n_events:
+            return self.run_event()
+        return self._event_sums(int(ncalls))
 
     def _run_iteration(self):
         """plain.py:37-43: sigma from (res2 * N - res^2) / (N - 1)."""

@@ -146,7 +146,9 @@ class VegasFlow(MonteCarloFlow):
 
     def _run_event(self, integrand, ncalls=None):
         """res, res2, arr_res2 of one chunk of ``ncalls`` events (vflow.py:389-430)."""
-        return self.run_event()
+        if ncalls is None or int(ncalls) == self.n_events:
+            return self.run_event()
+        return self._event_sums(int(ncalls))
 
     def _iteration_content(self):
         """Sample, reduce, sigma, refine (vflow.py:432-442) -- two kernel launches."""
