@@ -273,6 +273,7 @@ def test_run_event_and_device_run(kind):
     assert abs(float(res) - 1.0) < 5 * sig
     half = inst.device_run(n // 2)
     assert len(half) == 3 and abs(float(half[0]) - 0.5) < 5 * sig
+    assert abs(float(inst._run_event(None, n // 2)[0]) - 0.5) < 5 * sig
     assert inst.device_run(n, sent_pc=50.0)[0].shape == res.shape
     dev = inst.get_device()
     assert dev == inst.device and inst.get_device() is None
