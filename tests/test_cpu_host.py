@@ -202,3 +202,26 @@ def test_generate_condition_function():
     for args in ((1, "and"), (5, "bad_condition"), (5, ["or", "and"]), (3, ["or", "bad_condition"])):
         with pytest.raises(ValueError):
             generate_condition_function(*args)
+
+
+def test_state_buffer_layout():
+    """Average, flags word and history rows share one float64 buffer (one D2H copy
+    per run_integration); growing the history keeps what is there."""
+    inst = VegasFlow(2, 100, verbose=False, device="cpu")
+    ws = inst._workspace()
+    state = ws["state"]
+    assert ws["avg"].data_ptr() == state.data_ptr()
+    assert ws["flags"].dtype == torch.int32 and ws["flags"].numel() == 2
+    assert ws["flags"].data_ptr() == state[5:6].data_ptr()
+    assert ws["history"].data_ptr() == state[6:].data_ptr() and tuple(ws["history"].shape) == (16, 2)
+    ws["avg"][:] = torch.arange(5, dtype=torch.float64)
+    ws["flags"][0] = 4
+    ws["history"][3] = torch.tensor([1.5, 0.25], dtype=torch.float64)
+    host = state[: 5 + 1 + 4 * 2].numpy()
+    assert int(host[5:6].view(np.int32)[0]) == 4
+    np.testing.assert_array_equal(host[6:].reshape(4, 2)[3], [1.5, 0.25])
+    inst._state_rows(ws, 64)
+    assert tuple(ws["history"].shape) == (64, 2)
+    np.testing.assert_array_equal(ws["avg"].numpy(), np.arange(5.0))
+    assert int(ws["flags"][0]) == 4
+    np.testing.assert_array_equal(ws["history"][3].numpy(), [1.5, 0.25])
