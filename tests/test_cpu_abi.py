@@ -63,3 +63,14 @@ def test_constants_match_header():
         m = re.search(rf"#define\s+{name}\s+(\d+)", text)
         assert m, name
         assert getattr(nat, name) == int(m.group(1)), name
+
+
+def test_binding_argument_counts_match_header():
+    """Every ctypes signature has as many arguments as the C prototype."""
+    from vegasflow_gb300 import _native
+
+    text = open(HEADER).read()
+    for m in re.finditer(r"^(?:int|const char\*)\s+(vf_\w+)\s*\((.*?)\);", text, re.M | re.S):
+        name, params = m.group(1), " ".join(m.group(2).split())
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert len(_native.SIGNATURES[name]) == n, (name, n, len(_native.SIGNATURES[name]))
