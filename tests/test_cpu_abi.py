@@ -74,3 +74,23 @@ def test_binding_argument_counts_match_header():
         name, params = m.group(1), " ".join(m.group(2).split())
         n = 0 if params in ("", "void") else params.count(",") + 1
         assert len(_native.SIGNATURES[name]) == n, (name, n, len(_native.SIGNATURES[name]))
+
+
+def test_binding_argument_types_match_header():
+    """Pointers bind as pointers, and each scalar with the ctypes type of its C type."""
+    from vegasflow_gb300 import _native
+
+    scalar = {"int": ctypes.c_int, "double": ctypes.c_double, "long long": ctypes.c_longlong,
+              "unsigned long long": ctypes.c_ulonglong, "unsigned int": ctypes.c_uint}
+    text = open(HEADER).read()
+    for m in re.finditer(r"^(?:int|const char\*)\s+(vf_\w+)\s*\((.*?)\);", text, re.M | re.S):
+        name, params = m.group(1), " ".join(m.group(2).split())
+        if params in ("", "void"):
+            continue
+        for k, (param, bound) in enumerate(zip(params.split(","), _native.SIGNATURES[name])):
+            param = param.strip()
+            if "*" in param:
+                assert bound in (ctypes.c_void_p, ctypes.c_char_p), (name, k, param)
+            else:
+                ctype = " ".join(t for t in param.split()[:-1] if t != "const")
+                assert bound is scalar[ctype], (name, k, param, bound)
