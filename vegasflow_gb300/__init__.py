@@ -9,11 +9,7 @@ Drop-in names (vegasflow __init__.py:3-8): ``VegasFlow``, ``PlainFlow``,
 from .configflow import DTYPE, DTYPEINT, float_me, int_me, run_eager
 from .plain import PlainFlow, plain_sampler, plain_wrapper
 from .vflow import VegasFlow, vegas_sampler, vegas_wrapper
+from .vflowplus import VegasFlowPlus, vegasflowplus_sampler, vegasflowplus_wrapper
 from . import integrands
-
-try:
-    from .vflowplus import VegasFlowPlus, vegasflowplus_sampler, vegasflowplus_wrapper
-except ImportError:  # pragma: no cover - added with the VEGAS+ kernels
-    pass
 
 __version__ = "1.4.0+gb300"

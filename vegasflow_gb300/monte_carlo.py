@@ -5,9 +5,13 @@ events_limit, list_devices, verbose, xmin, xmax)``, ``compile(integrand,
 compilable, signature, trace, check)``, ``run_integration(n_iter, log_time,
 histograms)``, ``run_event``, ``generate_random_array``, ``set_seed``, the
 ``n_events`` / ``events_per_run`` / ``history`` / ``xjac`` properties, and the
-``wrapper`` / ``sampler`` helpers.  Extra keyword arguments: ``precision``
-("fp64" = the reference's float64 arithmetic, "fp32" = the fused fp32 form),
-``device`` and ``seed``.
+``wrapper`` / ``sampler`` helpers, ``make_differentiable`` and the device-pool
+methods (``get_device`` / ``release_device`` / ``device_run`` over the one GPU).
+Extra keyword arguments: ``precision`` ("fp64" = the reference's float64
+arithmetic, "fp32" = the fused fp32 form), ``device``, ``seed``, ``autotune``
+(time the fp32 sampler's launch shapes on the workload and cache the winner) and
+``cuda_graph`` (iterations of device integrands as replays of one captured CUDA
+graph).
 
 Execution model (one GPU):
   * an integrand built with ``vegasflow_gb300.integrands`` runs *inside* the
