@@ -1,7 +1,8 @@
 // Iteration-end work: reduce the per-block partial rows in a fixed order,
 // sigma, the running 1/sigma^2-weighted average and chi^2, and the grid
-// refinement (one block per dimension).  Also the standalone refinement, the
-// per-bin histogram utility and the reduction for torch-evaluated integrands.
+// refinement (a cluster of 8 blocks per dimension, block 0 refining the row).
+// Also the standalone refinement, the per-bin histogram utility and the
+// reduction for torch-evaluated integrands.
 #pragma once
 #include "vf_device.cuh"
 #include "vf_refine.cuh"
