@@ -225,3 +225,15 @@ def test_state_buffer_layout():
     np.testing.assert_array_equal(ws["avg"].numpy(), np.arange(5.0))
     assert int(ws["flags"][0]) == 4
     np.testing.assert_array_equal(ws["history"][3].numpy(), [1.5, 0.25])
+
+
+@pytest.mark.parametrize("name", ["f", "x", "w", "p"])
+def test_cuda_integrand_any_function_name(name):
+    """A user function may be named like a sampler local (f, x, w, ...): the
+    samplers reach it through a global-scope wrapper."""
+    src = (f"__device__ vf_real {name}(const vf_real* y, int n_dim, vf_real weight, const double* q) "
+           "{ vf_real r = 1; for (int d = 0; d < n_dim; ++d) r *= y[d]; return r; }")
+    f = integrands.cuda_integrand(src, name)
+    for alg, prec in ((0, 1), (0, 0), (2, 1), (3, 1)):
+        ok, log = f.check(alg, prec, 3)
+        assert ok, (name, alg, prec, log)

@@ -80,7 +80,12 @@ std::string program_text(const char* source, const char* func_name, int alg, int
   std::string src = "#define VF_JIT_USER 1\n";
   src += std::string("typedef ") + real + " vf_real;\n";
   src += source;
-  src += "\n#define VF_USER_FN " + std::string(func_name) + "\n";
+  // the samplers call the user function through a global-scope wrapper with an
+  // unusual name: a kernel local (f, x, w, ...) cannot shadow it there
+  src += "\n__device__ __forceinline__ vf_real vf_user_integrand_call_(const vf_real* vf_x_, int vf_n_, "
+         "vf_real vf_w_, const double* vf_p_) { return " +
+         std::string(func_name) + "(vf_x_, vf_n_, vf_w_, vf_p_); }\n";
+  src += "#define VF_USER_FN vf_user_integrand_call_\n";
   exprs->clear();
   if (alg == VF_ALG_BATCH) {
     src += "#include \"vf_batch_sampler.cuh\"\n";
