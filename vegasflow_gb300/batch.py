@@ -224,13 +224,16 @@ class VegasBatch:
         return avg[:, 2].copy(), avg[:, 3].copy(), avg[:, 4].copy(), int(host[-1])
 
     def history_host(self):
+        """(integrals, iterations, 2) array of every integral's (res, sigma) per iteration."""
         return self.history[:, : self.iterations_done].cpu().numpy()
 
     def grid(self, i):
+        """The current (n_dim, 51) grid of integral ``i`` (a view of the device buffer)."""
         off = int(self._grid_off[i])
         return self.grids[off: off + self.dims[i] * (BINS_MAX + 1)].reshape(self.dims[i], BINS_MAX + 1)
 
     def total_events(self):
+        """Events per iteration over all integrals."""
         return int(sum(self.events))
 
 

@@ -54,6 +54,10 @@ PARAMS_PER_SLOT = 2 * MAX_DIM + 2
 
 @dataclass
 class Request:
+    """One integration request: integrand, n_dim, events per iteration, the target
+    relative sigma and iteration cap, its arrival time (seconds) and optional timeout;
+    the server fills in the result, status and timings."""
+
     n_dim: int
     n_events: int
     integrand: DeviceIntegrand
@@ -148,6 +152,7 @@ def request_footprint(n_dim, n_events, tile_events=DEFAULT_TILE_EVENTS, hist_cap
 
 
 def percentile(values, q):
+    """The ``q``-th percentile of ``values`` (NaN for an empty list)."""
     v = np.sort(np.asarray(values, dtype=np.float64))
     if v.size == 0:
         return float("nan")
