@@ -288,18 +288,25 @@ int vf_consume_array_into_indices(const double* input, const int* indices, long 
  * captured, fixed-budget deployments.  The block-partial scratch lives in a
  * 4 MiB file-scope __device__ array inside the library (held by every GPU that
  * loads it until exit); the caller passes only inputs (grid [n_dim][51],
- * params) and the output res_sigma (device [2]: result, sigma).
+ * params) and outputs: res_sigma (device [2]: result, sigma) and, when not
+ * NULL, flags_out (device int: this call's VF_FLAG_* bits, 0 when nothing went
+ * wrong -- VF_FLAG_NONFINITE for a NaN/Inf sum, VF_FLAG_REFINE_OVERRUN from the
+ * refinement).  train: 0 no histogram and no refinement, 1 float64 refinement,
+ * 2 float32 refinement (as the fp32 integrators refine); other values are
+ * rejected before anything is enqueued.
  *
  * Limits: n_dim 1..16 and a built-in integrand id; xjac = 1/n_events, no
  * integration limits, no per-event taps.  The first call on a device resolves
- * the scratch's device address (cudaGetSymbolAddress): make that first call
- * before any stream capture.  All calls share the scratch and it keeps the last
- * call's contents (the state that must start at zero is cleared per call);
- * calls that overlap on the GPU race on it and must be ordered by the caller.
+ * the scratch's device address (cudaGetSymbolAddress), and so does the first
+ * call after a device reset (a new context): make that call before any stream
+ * capture.  All calls share the scratch and it keeps the last call's contents
+ * (the state that must start at zero is cleared per call); calls that overlap
+ * on the GPU race on it and must be ordered by the caller.
  */
 int vf_vegas_iteration_static(int precision, double* grid, int n_dim, long long n_events,
                               unsigned long long seed, unsigned int call_ctr, int integrand,
-                              const double* params, int train, double* res_sigma, void* stream);
+                              const double* params, int train, double* res_sigma, int* flags_out,
+                              void* stream);
 
 /*
  * User integrands as CUDA device functions (replaces the TF custom-op route of

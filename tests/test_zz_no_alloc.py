@@ -40,6 +40,7 @@ def test_static_iteration_matches_regular_path(precision, rtol, grid_atol):
     grid_regular = grid_static.clone()
     params = torch.tensor([0.1, (1.0 / 0.1 / np.sqrt(np.pi)) ** n_dim], dtype=torch.float64, device=dev)
     out = torch.zeros(2, dtype=torch.float64, device=dev)
+    flags = torch.full((1,), -1, dtype=torch.int32, device=dev)
     stream = nat.stream_handle()
 
     rows = ctypes.c_int(0)
@@ -51,9 +52,10 @@ def test_static_iteration_matches_regular_path(precision, rtol, grid_atol):
 
     for call in (0, 1):
         rc = lib.vf_vegas_iteration_static(precision, _p(grid_static), n_dim, n_events, seed, call,
-                                           nat.VF_INT_SYMGAUSS, _p(params), 1, _p(out), stream)
+                                           nat.VF_INT_SYMGAUSS, _p(params), 1, _p(out), _p(flags), stream)
         assert rc == nat.VF_OK, lib.vf_last_error_string()
         got = out.cpu().numpy().copy()
+        assert int(flags.item()) == 0  # written by every call, nothing went wrong
 
         nat.check(lib.vf_sample(nat.VF_ALG_VEGAS, precision, _p(grid_regular), n_dim, n_events, 0,
                                 1.0 / n_events, None, None, 1.0, None, seed, call, nat.VF_INT_SYMGAUSS,
@@ -75,6 +77,36 @@ def test_static_iteration_rejects_unsupported_sizes():
     grid = torch.zeros((17, 51), dtype=torch.float64, device=dev)
     out = torch.zeros(2, dtype=torch.float64, device=dev)
     rc = lib.vf_vegas_iteration_static(nat.VF_PREC_F64, _p(grid), 17, 1000, 1, 0, nat.VF_INT_PROD, None,
-                                       1, _p(out), nat.stream_handle())
+                                       1, _p(out), None, nat.stream_handle())
     assert rc == nat.VF_ERR_UNSUPPORTED
     assert b"n_dim" in lib.vf_last_error_string()
+    # train outside 0..2 is refused before anything reaches the stream
+    grid4 = torch.tensor(np.linspace(0.0, 1.0, 51)[None, :].repeat(4, 0), device=dev)
+    rc = lib.vf_vegas_iteration_static(nat.VF_PREC_F32, _p(grid4), 4, 1000, 1, 0, nat.VF_INT_PROD, None,
+                                       3, _p(out), None, nat.stream_handle())
+    assert rc == nat.VF_ERR_ARG
+    assert b"train" in lib.vf_last_error_string()
+
+
+@pytest.mark.parametrize("precision", [nat.VF_PREC_F64, nat.VF_PREC_F32])
+def test_static_iteration_reports_device_flags(precision):
+    """A non-finite sum reaches the caller through flags_out (an infinite
+    normalisation makes every weight infinite), and the next clean call writes 0."""
+    lib = nat.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n_dim, n_events = 4, 100_000
+    grid = torch.tensor(np.linspace(0.0, 1.0, 51)[None, :].repeat(n_dim, 0), device=dev)
+    out = torch.zeros(2, dtype=torch.float64, device=dev)
+    flags = torch.zeros(1, dtype=torch.int32, device=dev)
+    bad = torch.tensor([0.1, float("inf")], dtype=torch.float64, device=dev)
+    rc = lib.vf_vegas_iteration_static(precision, _p(grid), n_dim, n_events, 5, 0, nat.VF_INT_SYMGAUSS,
+                                       _p(bad), 0, _p(out), _p(flags), nat.stream_handle())
+    assert rc == nat.VF_OK, lib.vf_last_error_string()
+    assert int(flags.item()) & nat.VF_FLAG_NONFINITE
+    good = torch.tensor([0.1, (1.0 / 0.1 / np.sqrt(np.pi)) ** n_dim], dtype=torch.float64, device=dev)
+    rc = lib.vf_vegas_iteration_static(precision, _p(grid), n_dim, n_events, 5, 1, nat.VF_INT_SYMGAUSS,
+                                       _p(good), 0, _p(out), _p(flags), nat.stream_handle())
+    assert rc == nat.VF_OK, lib.vf_last_error_string()
+    assert int(flags.item()) == 0
+    res, sigma = out.cpu().numpy()
+    assert abs(res - 1.0) < 6 * sigma
