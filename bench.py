@@ -19,8 +19,10 @@ HBM inputs (uniforms come from the in-kernel Philox stream).  Under torchrun
 value is the events of all ranks divided by the slowest rank's time.
 
 ``--impl reference`` times the reference algorithm's CPU restatement (the
-oracle: TensorFlow is not available on the host) on all host threads, over a
-bounded sample of the same workload per step.
+oracle: TensorFlow is not available on the host) on all host threads: each step
+is one whole float64 iteration (refinement included) of one 1e6-event chunk per
+thread, a bounded sample of the same workload.  The GPU arm's ``cpu_baseline``
+runs the same procedure.
 """
 
 from __future__ import annotations
@@ -43,6 +45,7 @@ N_DIM = 8
 A_WIDTH = 0.1
 EVENTS = 100_000_000
 L2_FLUSH_BYTES = 512 << 20
+CPU_BASELINE_STEPS = 8  # timed CPU iterations of the GPU arm's cpu_baseline (~10 s on 16 cores)
 
 # Algorithmic instruction budget of one event of the fused fp32 sampler at
 # n_dim = 8 (VEGAS map, Gaussian, compensated sums, histogram): counted from the
@@ -180,20 +183,42 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ reference arm
-def cpu_oracle_rate(n_events, threads, seed=0):
-    """One float64 VegasFlow iteration of the 8-D Gaussian on the host (the
-    oracle restatement of the reference), on `threads` threads."""
-    import numpy as np
+CPU_CHUNK = 1_000_000  # the reference's default events_limit (configflow.py:22)
 
-    import oracle
 
-    grid = oracle.initial_grid(N_DIM)
-    t0 = time.perf_counter()
-    res, sigma, arr = oracle.threaded_vegas_iteration(
-        grid, n_events, lambda x: oracle.integrand_symgauss(x, A_WIDTH), seed, threads)
-    dt = time.perf_counter() - t0
-    _ = oracle.refine_grid(arr, grid)
-    return n_events / dt, dt, res, sigma
+class CpuVegas:
+    """The float64 VegasFlow iteration of the 8-D Gaussian on the host cores,
+    through the oracle (the reference's algorithm restated in NumPy; TensorFlow,
+    which the reference runs on, is not installed on the host).  One step is one
+    whole iteration of ``threads`` chunks of ``CPU_CHUNK`` events -- one chunk
+    per thread, so every thread counted in ``cores`` works -- including the map,
+    the integrand, the sums, the histogram and the grid refinement; the grid
+    carries over from step to step as in a run of several iterations."""
+
+    def __init__(self, threads):
+        import oracle
+
+        self.oracle = oracle
+        self.threads = threads
+        self.events = threads * CPU_CHUNK
+        self.grid = oracle.initial_grid(N_DIM)
+
+    def step(self, seed):
+        o = self.oracle
+        t0 = time.perf_counter()
+        res, sigma, arr = o.threaded_vegas_iteration(
+            self.grid, self.events, lambda x: o.integrand_symgauss(x, A_WIDTH), seed, self.threads,
+            chunk=CPU_CHUNK)
+        self.grid = o.refine_grid(arr, self.grid)
+        return time.perf_counter() - t0, res, sigma
+
+    def describe(self, steps):
+        return {"kind": "port", "cores": self.threads, "threads_busy": self.threads,
+                "sample_events_per_step": self.events,
+                "sample": f"{steps} VegasFlow iterations x {self.events:.1e} events of the 8-D Gaussian "
+                          f"({self.threads} chunks of {CPU_CHUNK:.0e}, one per host thread), float64 oracle "
+                          "(NumPy, PCG64 uniforms through the TECH_CUT affine), grid refined inside the "
+                          "timed step"}
 
 
 def host_threads():
@@ -203,42 +228,38 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+def cpu_baseline_run(steps, warmup, seed0=0):
+    """Timed CPU steps: (events/s, seconds per step, CpuVegas)."""
+    cpu = CpuVegas(host_threads())
+    for w in range(warmup):
+        cpu.step(seed0 + 1000 + w)
+    times = [cpu.step(seed0 + k)[0] for k in range(steps)]
+    return cpu.events * len(times) / sum(times), times, cpu
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    threads = host_threads()
-    sample = 4_000_000
-    for _ in range(max(0, args.warmup)):
-        cpu_oracle_rate(1_000_000, threads)
-    rates, times = [], []
-    for k in range(args.steps):
-        r, dt, _, _ = cpu_oracle_rate(sample, threads, seed=k)
-        rates.append(r)
-        times.append(dt)
-    value = sample * len(times) / sum(times)
+    value, times, cpu = cpu_baseline_run(args.steps, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (NumPy PCG64 uniforms through the TECH_CUT affine)",
-        "config": workload_config(args, sample_events=sample),
-        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} iterations x {sample:.0e} events of the 8-D Gaussian, "
-                                   "float64 VegasFlow oracle, NumPy on host threads"},
+        "config": workload_config(args),
+        "cpu_baseline": dict(cpu.describe(args.steps), value=value, unit="events/s"),
         "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def workload_config(args, sample_events=None):
-    cfg = {"workload": "8-D Gaussian a=0.1, VegasFlow importance sampling (grid trained every "
-                       "iteration), 50 bins, 1e8 events/iteration",
-           "n_dim": N_DIM, "events_per_iteration": args.events, "bins": 50,
-           "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
-           "l2": "no HBM inputs (in-kernel Philox); L2 flushed (512 MB write) between timed iterations"}
-    if sample_events:
-        cfg["sample_events_per_step"] = sample_events
-    return cfg
+def workload_config(args):
+    return {"workload": "8-D Gaussian a=0.1, VegasFlow importance sampling (grid trained every "
+                        "iteration), 50 bins, 1e8 events/iteration",
+            "n_dim": N_DIM, "events_per_iteration": args.events, "bins": 50,
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
+            "l2": "GPU arm: in-kernel Philox uniforms (no HBM inputs), L2 flushed by a 512 MB write "
+                  "between timed iterations; CPU arms: host memory"}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -374,13 +395,9 @@ def main():
     if args.serving_seconds > 0:
         line["serving"] = serving_run(args.serving_seconds)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = host_threads()
-        cpu_oracle_rate(500_000, threads)
-        rate, dt, _, _ = cpu_oracle_rate(8_000_000, threads, seed=1)
-        line["cpu_baseline"] = {"value": rate, "unit": "events/s", "cores": threads, "kind": "port",
-                                "sample": "1 iteration x 8e6 events of the 8-D Gaussian, float64 "
-                                          "VegasFlow oracle (NumPy) on the host threads",
-                                "seconds": dt}
+        rate, times, cpu = cpu_baseline_run(CPU_BASELINE_STEPS, 1)
+        line["cpu_baseline"] = dict(cpu.describe(len(times)), value=rate, unit="events/s",
+                                    seconds=float(sum(times)))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -461,7 +478,7 @@ def injected_run(dev, n_events, K, W, seed=11):
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": INJECTED_BYTES_PER_EVENT * n_events,
                      "traffic_note": "algorithmic bytes; ncu dram__bytes (read + write) on a 1e7-event "
-                                     "launch equals them to within 1% (profiles/vegas_fp32_injected.md)",
+                                     "launch equals them to within 1%",
                      "peak_source": source},
     }
 

@@ -99,7 +99,11 @@ int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, 
  *  train     fill the per-bin histogram of (w f)^2
  *  partials  [rows][2 + 50 n_dim] block partials: stored (accumulate=0) or added
  *  ind_out, x_out, w_out, f_out  nullable per-event taps ([n][D] int32,
- *            [n][D] / [n] / [n] in the precision's type)
+ *            [n][D] / [n] / [n] in the precision's type).  An fp32 VEGAS launch
+ *            of VF_INT_SYMGAUSS or VF_INT_PROD with ind_out as its only tap runs
+ *            the fused fp32 sampler itself (its parity instantiation), so the
+ *            indices are those of the benchmarked kernel; other taps use the
+ *            generic sampler.
  *  flags     nullable device int receiving VF_FLAG_* bits
  */
 int vf_sample(int alg, int precision, const double* grid, int n_dim, long long n_events,
@@ -174,6 +178,9 @@ int vf_plus_rows(int precision, int n_dim, int n_hcubes, int* rows);
  * n_hcubes, the integrand, the per-hypercube sums ress/ress2
  * (segment_sum, vflowplus.py:206-214) and the histogram rows.  Philox counter =
  * the event's index within the iteration.  VF_INT_NONE samples only (taps).
+ * An fp32 launch of VF_INT_SYMGAUSS or VF_INT_BREIT_WIGNER with Philox uniforms,
+ * ind_out and optionally x_out as its taps runs the fp32 sampler itself (its
+ * parity instantiation); other taps use the float64-map sampler.
  */
 int vf_plus_sample(int precision, const double* grid, int n_dim, int n_strat, int n_hcubes,
                    const int* n_ev, const long long* ev_start, double xjac, const double* xmin,

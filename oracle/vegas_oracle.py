@@ -35,6 +35,8 @@ __all__ = [
     "OracleVegas", "OraclePlain", "OraclePlus", "INTEGRANDS", "integrand_symgauss",
     "integrand_gauss_mu", "integrand_breit_wigner", "integrand_prod", "integrand_sum",
     "symgauss_exact", "gauss_mu_exact", "breit_wigner_exact", "threaded_vegas_iteration",
+    "vegas_f32_table", "uniforms_of_words", "plus_bins_from_words", "hypercube_points",
+    "fma_f32",
 ]
 
 # configflow.py:13-24
@@ -528,28 +530,80 @@ def _f32_frac_from_lo(lo):
     return bits.view(np.float32) - np.float32(1.0)
 
 
-def vegas_map_f32_words(words, edges_f32):
-    """fp32 form of the importance map on one 32-bit word per dimension.
+def fma_f32(a, b, c):
+    """float32(a * b + c) with one rounding (a, b, c float32 arrays): the product
+    is exact in float64 (24 + 24 bits), the sum's float64 rounding error is
+    recovered by TwoSum and folded in as a round-to-odd of the float64 sum, after
+    which the conversion to float32 rounds as a single fused operation would."""
+    p = a.astype(np.float64) * b.astype(np.float64)
+    c64 = c.astype(np.float64)
+    s = p + c64
+    bb = s - p
+    err = (p - (s - bb)) + (c64 - bb)
+    even = (s.view(np.uint64) & np.uint64(1)) == 0
+    fix = (err != 0.0) & even
+    s = np.where(fix, np.nextafter(s, s + err), s)
+    return s.astype(np.float32)
 
-    With t = (~word + 1/2) / 2^32 standing for ``1 - u``: ``p = 50 * ~word + 25``
-    (exact, 64-bit), ``ind = p >> 32``, ``frac`` = top 23 bits of ``p mod 2^32``;
-    ``x = x_lo + delta * frac`` as one fused multiply-add (emulated in float64 and
-    rounded once), ``w = prod(delta)`` in float32 times 50^n_dim."""
+
+def vegas_f32_table(divisions):
+    """The per-bin table {c0, c1} of the fp32 VEGAS samplers without integration
+    limits: ``c1 = delta``, ``c0 = lo - delta``, each computed in float64 from the
+    grid and rounded once to float32 (so that ``x = c0 + c1 m`` for m in [1, 2))."""
+    g = np.asarray(divisions, dtype=np.float64)
+    lo = g[:, :-1]
+    dl = g[:, 1:] - lo
+    return (lo - dl).astype(np.float32), dl.astype(np.float32)
+
+
+def vegas_map_f32_words(words, divisions, xjac):
+    """fp32 form of the importance map on one 32-bit Philox word per dimension
+    (the fused sampler's and the map kernel's draw, no integration limits).
+
+    With t = (~word + 1/2) / 2^32 standing for ``1 - u``, u = (word + 1/2) / 2^32:
+    ``p = 50 * ~word + 25`` (exact, 64-bit) is 50 t 2^32, so ``ind = p >> 32`` is
+    the reference's ``int32(50 (1 - u))`` (vflow.py:117, :67; exact in float64 for
+    such u) and ``m = 1 + (top 23 bits of p mod 2^32) / 2^23`` its fraction plus 1.
+    ``x = fl32(c1 m + c0)`` (one fused multiply-add through the table of
+    ``vegas_f32_table``), ``w = prod_d c1`` in float32 left to right, times the
+    float32 constant ``xjac * 50^n_dim`` (its float64 product rounded once).
+    Returns (ind int32, x float32, w float32)."""
     words = np.asarray(words, dtype=np.uint32)
     n, n_dim = words.shape
     inv = (~words).astype(np.uint64)
     p = inv * np.uint64(50) + np.uint64(25)
     ind = (p >> np.uint64(32)).astype(np.int32)
-    frac = _f32_frac_from_lo((p & _MASK32).astype(np.uint32))
-    edges = np.asarray(edges_f32, dtype=np.float32)
-    lo = np.take_along_axis(edges, ind.T, axis=1).T
-    hi = np.take_along_axis(edges, ind.T + 1, axis=1).T
-    delta = (hi - lo).astype(np.float32)
-    x = (lo.astype(np.float64) + delta.astype(np.float64) * frac.astype(np.float64)).astype(np.float32)
-    w = delta[:, 0].copy()
+    mbits = ((p & _MASK32) >> np.uint64(9)).astype(np.uint32) | np.uint32(0x3F800000)
+    m = mbits.view(np.float32)
+    c0, c1 = vegas_f32_table(divisions)
+    c0e = np.take_along_axis(c0, ind.T, axis=1).T
+    c1e = np.take_along_axis(c1, ind.T, axis=1).T
+    x = fma_f32(c1e, m, c0e)
+    wf = c1e[:, 0].copy()
     for d in range(1, n_dim):
-        w = (w * delta[:, d]).astype(np.float32)
+        wf = (wf * c1e[:, d]).astype(np.float32)
+    ws = float(xjac)
+    for _ in range(n_dim):
+        ws *= 50.0
+    w = (wf * np.float32(ws)).astype(np.float32)
     return ind, x, w
+
+
+def uniforms_of_words(words):
+    """The float64 uniforms ``u = (word + 1/2) / 2^32`` that the fp32 samplers'
+    integer maps stand for (exact in float64)."""
+    return (np.asarray(words, dtype=np.float64) + 0.5) / 4294967296.0
+
+
+def plus_bins_from_words(words, points, n_strat):
+    """The fp32 VEGAS+ sampler's stratified bin per dimension, in exact integer
+    arithmetic: ``Q = 50 (p 2^32 + word) + 25`` is ``50 (p + u) 2^32`` for
+    u = (word + 1/2) / 2^32, and ``bin = (Q >> 32) div n_strat`` is
+    ``floor((p + u) 50 / n_strat)`` (vflowplus.py:72)."""
+    w = np.asarray(words, dtype=np.uint64)
+    p = np.asarray(points, dtype=np.uint64)
+    Q = ((p << np.uint64(32)) | w) * np.uint64(50) + np.uint64(25)
+    return ((Q >> np.uint64(32)) // np.uint64(int(n_strat))).astype(np.int32)
 
 
 def plain_map_f32_words(words):

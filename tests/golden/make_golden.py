@@ -2,7 +2,11 @@
 
 Usage (development container only; the reference tree must be present):
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py REFERENCE_ROOT
+    VEGASFLOW_REFERENCE=REFERENCE_ROOT python tests/golden/make_golden.py
+
+(REFERENCE_ROOT is the reference project's top directory, the one holding
+``src/vegasflow``.)
 
 The reference's ``src/vegasflow`` modules are imported unmodified, with
 ``tfshim`` installed as ``tensorflow`` (TensorFlow is not available here), and
@@ -12,7 +16,12 @@ on uniforms injected from ``numpy.random.default_rng(11)``.  Every raw uniform
 block the reference consumed is stored next to its outputs, so the tests replay
 exactly the same inputs through the oracle and the GPU kernels.
 
-Output: ``tests/golden/golden.npz`` (a few hundred KB).
+Output: ``tests/golden/golden.npz`` (a few hundred KB), ``reference_grid.json``
+(written by the reference's save_grid) and ``repo_grid.json`` (written by this
+project's save_grid and read back by the reference's load_grid).  With
+``--c2-precision`` it writes ``c2_precision.npz`` instead: the reference's
+float64 and float32 (``VEGASFLOW_FLOAT=32``) runs of the 8-D Gaussian on the
+same injected uniforms.
 """
 
 from __future__ import annotations
@@ -23,7 +32,12 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REPO = os.path.dirname(os.path.dirname(HERE))
+_args = [a for a in sys.argv[1:] if not a.startswith("--")]
+REF = _args[0] if _args else os.environ.get("VEGASFLOW_REFERENCE")
+if not REF or not os.path.isdir(os.path.join(REF, "src", "vegasflow")):
+    sys.exit("make_golden.py: give the reference project's root (holding src/vegasflow) as the "
+             "argument or in VEGASFLOW_REFERENCE")
 
 sys.path.insert(0, HERE)
 import tfshim  # noqa: E402
@@ -153,6 +167,84 @@ def vegasflow_final(hist):
     return aux_res / weight_sum, np.sqrt(1.0 / weight_sum)
 
 
+def grid_interchange(ref_inst):
+    """Grid JSON files across the two implementations (vflow.py:271-347): the
+    reference's save_grid writes ``reference_grid.json`` (its trained 4-D grid,
+    which this project's load_grid must read back exactly); this project's
+    save_grid writes ``repo_grid.json``, which the reference's load_grid reads --
+    what it loaded is stored for the tests."""
+    ref_inst.save_grid(os.path.join(HERE, "reference_grid.json"))
+    sys.path.insert(0, REPO)
+    from vegasflow_gb300 import VegasFlow as RepoVegas  # save/load run on the host device
+
+    rng = np.random.default_rng(77)
+    sub = np.linspace(0.0, 1.0, 51)
+    warped = np.stack([np.array(vflow.refine_grid_per_dimension(tf._t(rng.random(50) ** 4), tf._t(sub)))
+                       for _ in range(3)])
+    mine = RepoVegas(3, 1000, verbose=False, device="cpu")
+    mine.load_grid(numpy_grid=warped)
+    repo_file = os.path.join(HERE, "repo_grid.json")
+    mine.save_grid(repo_file)
+    ref3 = vflow.VegasFlow(3, 1000, verbose=False)
+    ref3.load_grid(file_name=repo_file)
+    loaded = np.array(ref3.divisions)
+    assert np.array_equal(loaded, warped)
+    OUT["interchange/repo_grid"] = warped
+    OUT["interchange/ref_loaded_repo_grid"] = loaded
+
+
+# -- C2 precision comparator: the reference in float64 and in its float32 mode
+C2P_N, C2P_ITERS, C2P_SEED = 10_000_000, 3, 11
+
+
+def c2_precision_child(out_path):
+    """One run of the reference (VEGASFLOW_FLOAT taken from the environment at
+    import) on C2's injected uniforms: 8-D Gaussian a = 0.1, C2P_N events per
+    iteration in the default 1e6-event chunks, C2P_ITERS trained iterations, the
+    raw uniforms of every iteration drawn from default_rng(C2P_SEED) in order."""
+    from vegasflow.configflow import DTYPE
+
+    rng = np.random.default_rng(C2P_SEED)
+    tfshim.set_uniform_source(lambda shape: rng.random(shape))
+
+    def gauss(xarr, weight=None):
+        a = tf.constant(0.1, dtype=DTYPE)
+        pref = tf.cast(tf.pow(1.0 / 0.1 / np.sqrt(np.pi), 8), dtype=DTYPE)
+        return pref * tf.exp(-tf.reduce_sum(tf.square((xarr - 0.5) / a), axis=1))
+
+    inst = vflow.VegasFlow(8, C2P_N, verbose=False)
+    inst.compile(gauss)
+    hist, grids = [], []
+    for _ in range(C2P_ITERS):
+        res, sig = inst._run_iteration()
+        hist.append((float(np.asarray(res)), float(np.asarray(sig))))
+        grids.append(np.array(inst.divisions, dtype=np.float64))
+    np.savez(out_path, history=np.array(hist), grids=np.stack(grids), dtype=str(np.dtype(DTYPE.as_numpy_dtype)))
+
+
+def c2_precision():
+    """Runs c2_precision_child in float64 and float32 processes and writes
+    ``c2_precision.npz``: the reference's naive float32 form set beside its
+    float64 result on the same raw uniforms."""
+    import subprocess
+    import tempfile
+
+    out = {"n_events": np.int64(C2P_N), "iterations": np.int64(C2P_ITERS), "seed": np.int64(C2P_SEED)}
+    with tempfile.TemporaryDirectory() as tmp:
+        for bits in ("64", "32"):
+            path = os.path.join(tmp, f"c2_{bits}.npz")
+            env = dict(os.environ, VEGASFLOW_FLOAT=bits)
+            subprocess.run([sys.executable, os.path.abspath(__file__), REF, f"--c2-child={path}"], env=env,
+                           check=True)
+            r = np.load(path)
+            out[f"f{bits}/history"] = r["history"]
+            out[f"f{bits}/grids"] = r["grids"]
+            assert str(r["dtype"]) == ("float64" if bits == "64" else "float32"), r["dtype"]
+    path = os.path.join(HERE, "c2_precision.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path}")
+
+
 def main():
     rng = np.random.default_rng(2024)
 
@@ -197,7 +289,8 @@ def main():
                                                                      tf._t(np.int32(50))))
 
     # -- full integrations through the public API
-    run_case("vegas4", lambda: vflow.VegasFlow(4, 2000, verbose=False), symgauss, 3)
+    inst4 = run_case("vegas4", lambda: vflow.VegasFlow(4, 2000, verbose=False), symgauss, 3)
+    grid_interchange(inst4)
     run_case("vegas4_chunks", lambda: vflow.VegasFlow(4, 1500, events_limit=400, verbose=False),
              symgauss, 2)
     run_case("vegas2_quirky", lambda: vflow.VegasFlow(2, 1000, verbose=False), quirky_gauss, 3)
@@ -233,4 +326,10 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    child = [a for a in sys.argv[1:] if a.startswith("--c2-child=")]
+    if child:
+        c2_precision_child(child[0].split("=", 1)[1])
+    elif "--c2-precision" in sys.argv:
+        c2_precision()
+    else:
+        main()

@@ -1,0 +1,173 @@
+"""Bin-index parity of the fp32 kernels that earn the benchmark numbers.
+
+The fused fp32 VEGAS sampler, its TMA injected-uniform path and the fp32
+VEGAS+ sampler each have a parity instantiation that writes every event's bin
+indices (reached through ``vf_sample`` / ``vf_plus_sample`` with ``ind_out`` as
+the only tap).  On the same Philox words the indices must equal the
+reference's float64 bins of the uniforms the words stand for,
+u = (word + 1/2) / 2^32 (``oracle.vegas_map`` / ``oracle.plus_map``, restating
+vflow.py:93-126, :67 and vflowplus.py:46-80, both pinned to the reference's
+own fixtures), and for injected float64 uniforms the reference's bins of those
+uniforms.  Bar: ``assert_array_equal`` on every index.  The map kernel of the
+sampler API (the same draw without an integrand) is also checked for its
+points (within 1 float32 ulp of the oracle's one-rounding restatement) and
+weights (bit-exact)."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from vegasflow_gb300 import VegasFlow, VegasFlowPlus, integrands
+from vegasflow_gb300 import _native as nat
+
+pytestmark = pytest.mark.gpu
+
+
+def _trained(n_dim, n, integrand, seed=31, iters=3):
+    inst = VegasFlow(n_dim, n, verbose=False, precision="fp32", seed=seed)
+    inst.compile(integrand)
+    inst.run_integration(iters)
+    return inst
+
+
+def _with_layout(layout, fn):
+    lib = nat.load()
+    old = ctypes.c_int(0)
+    nat.check(lib.vf_tune_get(nat.VF_TUNE_F32_HIST_COPIES, ctypes.byref(old)))
+    nat.check(lib.vf_tune_set(nat.VF_TUNE_F32_HIST_COPIES, layout))
+    try:
+        return fn()
+    finally:
+        nat.check(lib.vf_tune_set(nat.VF_TUNE_F32_HIST_COPIES, old.value))
+
+
+def _reference_bins(u, grid, chunk=1_000_000):
+    out = np.empty(u.shape, dtype=np.int32)
+    for s in range(0, u.shape[0], chunk):
+        _, _, out[s:s + chunk] = oracle.vegas_map(u[s:s + chunk], grid)
+    return out
+
+
+@pytest.mark.parametrize("n_dim", [1, 3, 8, 16])
+@pytest.mark.parametrize("layout", [0, 8])
+@pytest.mark.parametrize("which", ["symgauss", "prod"])
+def test_fused_sampler_bins_are_the_reference_bins(n_dim, layout, which):
+    """Philox path: D = 1, 3 take the two-events-per-pass loop, D = 8, 16 the
+    single one; layout 8 (fixed point) adds the scale-setting first event."""
+    n, call = 1_000_000, 7
+    f = integrands.symgauss(0.2) if which == "symgauss" else integrands.prod()
+    inst = _trained(n_dim, n, f)
+    ind = torch.full((n, n_dim), -1, dtype=torch.int32, device="cuda")
+    _with_layout(layout, lambda: inst._sample(n, 0, call, inst._int_id, inst._params_dev, True, False, ind=ind))
+    torch.cuda.synchronize()
+    words = oracle.philox_words(inst._seed, call, 0, n, n_dim)
+    want = _reference_bins(oracle.uniforms_of_words(words), inst.divisions.cpu().numpy())
+    np.testing.assert_array_equal(ind.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("n_dim", [1, 3, 8, 16])
+def test_map_kernel_points_and_weights_match_oracle(n_dim):
+    n, call = 1_000_000, 5
+    inst = _trained(n_dim, n, integrands.symgauss(0.2))
+    x = torch.empty((n, n_dim), dtype=torch.float32, device="cuda")
+    w = torch.empty(n, dtype=torch.float32, device="cuda")
+    ind = torch.empty((n, n_dim), dtype=torch.int32, device="cuda")
+    inst._sample(n, 0, call, nat.VF_INT_NONE, None, False, False, ind=ind, x=x, w=w)
+    torch.cuda.synchronize()
+    words = oracle.philox_words(inst._seed, call, 0, n, n_dim)
+    grid = inst.divisions.cpu().numpy()
+    ind_o, x_o, w_o = oracle.vegas_map_f32_words(words, grid, inst.xjac)
+    np.testing.assert_array_equal(ind.cpu().numpy(), ind_o)
+    np.testing.assert_array_equal(ind_o, _reference_bins(oracle.uniforms_of_words(words), grid))
+    xg = x.cpu().numpy()
+    assert np.all(xg >= 0) and np.all(x_o >= 0)  # the int32 views of non-negative floats are ordered
+    ulps = np.abs(xg.view(np.int32).astype(np.int64) - x_o.view(np.int32).astype(np.int64))
+    assert ulps.max() <= 1, ulps.max()
+    np.testing.assert_array_equal(w.cpu().numpy(), w_o)
+
+
+def _near_edge_uniforms(n_dim):
+    """Uniforms a few float64 ulps around every bin edge 1 - k/50 (k = 1..49)
+    and near the ends of the reference's range [1e-8, 1 - 1e-8)."""
+    vals = []
+    for k in range(1, 50):
+        x = y = 1.0 - k / 50.0
+        vals.append(x)
+        for _ in range(40):
+            x = np.nextafter(x, 2.0)
+            y = np.nextafter(y, -1.0)
+            vals += [x, y]
+    vals += [1e-8, np.nextafter(1e-8, 1.0), 1.0 - 1e-8, np.nextafter(1.0 - 1e-8, 0.0), 2.0 ** -12,
+             np.nextafter(2.0 ** -12, 0.0), 2.0 ** -13]
+    vals = np.array(vals)
+    rows = (vals.size + n_dim - 1) // n_dim
+    return np.resize(vals, rows * n_dim).reshape(rows, n_dim)
+
+
+@pytest.mark.parametrize("n_dim,n,misalign", [(8, 10_000_000, False), (16, 1_000_000, False),
+                                              (4, 1_000_000, False), (8, 1_000_000, True),
+                                              (5, 1_000_000, False)])
+def test_injected_fused_bins_are_the_reference_bins(n_dim, n, misalign):
+    """C2's injected mode (default_rng(11) through the TECH_CUT affine) with the
+    near-edge uniforms first: the TMA path (D = 4, 8, 16 on an aligned array)
+    and the plain-load path (misaligned, or D = 5)."""
+    u = oracle.tech_cut_affine(np.random.default_rng(11).random((n, n_dim)))
+    edge = _near_edge_uniforms(n_dim)
+    u[:edge.shape[0]] = edge
+    inst = _trained(n_dim, n, integrands.symgauss(0.2), iters=2)
+    if misalign:
+        buf = torch.empty(n * n_dim + 1, dtype=torch.float64, device="cuda")
+        ud = buf[1:].view(n, n_dim)
+        ud.copy_(torch.as_tensor(u, device="cuda"))
+        assert ud.data_ptr() % 16 == 8
+    else:
+        ud = torch.as_tensor(u, device="cuda").contiguous()
+        assert ud.data_ptr() % 16 == 0
+    ind = torch.full((n, n_dim), -1, dtype=torch.int32, device="cuda")
+    ws = inst._workspace()
+    ws["flags"].zero_()
+    inst._sample(n, 0, 0, inst._int_id, inst._params_dev, True, False, u_inj=ud, ind=ind)
+    torch.cuda.synchronize()
+    assert int(ws["flags"][0].item()) == 0
+    np.testing.assert_array_equal(ind.cpu().numpy(), _reference_bins(u, inst.divisions.cpu().numpy()))
+
+
+@pytest.mark.parametrize("n_dim,n_events,adaptive,which", [(6, 2_000_000, True, "bw"),
+                                                           (3, 200_000, False, "symgauss"),
+                                                           (2, 100_000, True, "symgauss"),
+                                                           (9, 300_000, False, "bw")])
+def test_plus_fp32_bins_are_the_reference_bins(n_dim, n_events, adaptive, which):
+    """The fp32 VEGAS+ sampler's integer stratified map on a trained grid and a
+    reallocated event layout (C3: 6-D Breit-Wigner, adaptive, 2e6 events)."""
+    if which == "bw":
+        f = integrands.breit_wigner(np.random.default_rng(3).random(n_dim - 1))
+    else:
+        f = integrands.symgauss(0.2)
+    inst = VegasFlowPlus(n_dim, n_events, adaptive=adaptive, verbose=False, precision="fp32", seed=13)
+    inst.compile(f)
+    inst.run_integration(2)
+    n_total = int(inst.n_events)
+    n_ev = inst.n_ev.cpu().numpy()
+    assert int(n_ev.sum()) == n_total
+    ind = torch.full((n_total, n_dim), -1, dtype=torch.int32, device="cuda")
+    x = torch.empty((n_total, n_dim), dtype=torch.float32, device="cuda")
+    ws = inst._plus_buffers()
+    call = 9
+    nat.call("vf_plus_sample", nat.VF_PREC_F32, nat.ptr(inst.divisions), n_dim, inst._n_strat, inst._n_hcubes,
+             nat.ptr(inst.n_ev), nat.ptr(inst._ev_start), float(inst.xjac), None, None, 1.0, None, inst._seed,
+             call, inst._int_id, nat.ptr(inst._params_dev), 0, nat.ptr(ws["ress"]), nat.ptr(ws["ress2"]),
+             nat.ptr(ws["partials"]), inst._rows, nat.ptr(ind), nat.ptr(x), None, None, nat.stream_handle())
+    torch.cuda.synchronize()
+    words = oracle.philox_words(inst._seed, call, 0, n_total, n_dim)
+    grid = inst.divisions.cpu().numpy()
+    x64, _, want, _ = oracle.plus_map(oracle.uniforms_of_words(words), inst._n_strat, n_ev, grid)
+    got = ind.cpu().numpy()
+    np.testing.assert_array_equal(got, want)
+    h = np.repeat(np.arange(inst._n_hcubes), n_ev)
+    pts = oracle.hypercube_points(inst._n_hcubes, inst._n_strat, n_dim)[h]
+    np.testing.assert_array_equal(got, oracle.plus_bins_from_words(words, pts, inst._n_strat))
+    # the points: float32 through the per-bin table, within 2e-6 of the float64 map
+    assert np.max(np.abs(x.cpu().numpy().astype(np.float64) - x64)) < 2e-6

@@ -306,14 +306,19 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
     return fail(VF_ERR_ARG, "vf_sample: partials/rows required when evaluating");
   if (rows < 1) rows = 1;
   const bool taps = ind_out || x_out || w_out || f_out;
-  const bool fast = !jit && use_vegas_f32(alg, precision, integrand, taps);
+  // bin indices as the only tap of an fp32 VEGAS launch with the symmetric
+  // Gaussian or the product integrand: the fused sampler's parity instantiation
+  const bool tap_fast = !jit && ind_out && !x_out && !w_out && !f_out && precision == VF_PREC_F32 &&
+                        alg == VF_ALG_VEGAS && (integrand == VF_INT_SYMGAUSS || integrand == VF_INT_PROD);
+  const bool fast = !jit && (use_vegas_f32(alg, precision, integrand, taps) || tap_fast);
   // the fp32 VEGAS map alone (no integrand, Philox uniforms): x, w, indices to HBM
   const bool map_only = !jit && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS && integrand == VF_INT_NONE &&
                         !u_inj && !f_out && (x_out || w_out || ind_out);
-  const int threads = fast ? g_f32_threads.load() : VF_THREADS;
-  const void* k = jit ? nullptr
-                      : (fast ? vf::vegas_f32_kernel(n_dim, integrand, threads)
-                              : sample_kernel(precision, n_dim, integrand));
+  const int threads = tap_fast ? 256 : (fast ? g_f32_threads.load() : VF_THREADS);
+  const void* k = jit        ? nullptr
+                  : tap_fast ? vf::vegas_f32_tap_kernel(n_dim, integrand)
+                  : fast     ? vf::vegas_f32_kernel(n_dim, integrand, threads)
+                             : sample_kernel(precision, n_dim, integrand);
   if (!k && !jit) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no kernel for this configuration");
 
   vf::SampleArgs a;

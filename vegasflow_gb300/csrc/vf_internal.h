@@ -22,9 +22,16 @@ inline const void* vegas_f32_kernel(int n_dim, int integrand, int threads = 256)
   return n_dim <= 8 ? vegas_f32_kernel_a256(n_dim, integrand) : vegas_f32_kernel_b256(n_dim, integrand);
 }
 
+// The parity instantiation of the fp32 VEGAS sampler (256 threads; writes each
+// event's bin indices): VF_INT_SYMGAUSS and VF_INT_PROD, dimensions 1..16.
+const void* vegas_f32_tap_kernel(int n_dim, int integrand);
+
 // The fp32 VEGAS+ sampler for built-in integrands, specialised on the
 // dimension count (Philox uniforms; 256 threads per block).
 const void* plus_f32_kernel(int n_dim, int integrand);
+// Its parity instantiation (writes bin indices and float32 points):
+// VF_INT_SYMGAUSS and VF_INT_BREIT_WIGNER, dimensions 1..16.
+const void* plus_f32_tap_kernel(int n_dim, int integrand);
 
 // The fp32 VEGAS map kernel without an integrand (x, w, bin indices to HBM),
 // specialised on the dimension count; 256 threads per block.

@@ -143,9 +143,14 @@ int plus_sample_impl(int precision, const double* grid, int n_dim, int n_strat, 
   if ((integrand == VF_INT_SYMGAUSS || integrand == VF_INT_GAUSS || integrand == VF_INT_BREIT_WIGNER) && !params)
     return err(VF_ERR_ARG, "vf_plus_sample: integrand needs params");
   // fp32 with a built-in integrand and Philox uniforms: the float32 kernel
-  const bool f32 = precision == VF_PREC_F32 && integrand >= VF_INT_SYMGAUSS && integrand <= VF_INT_SUM &&
-                   !u_inj && !ind_out && !x_out && !w_out;
-  const void* k = jit ? nullptr : (f32 ? vf::plus_f32_kernel(n_dim, integrand) : plus_kernel(precision, n_dim, integrand));
+  const bool f32_tap = !jit && precision == VF_PREC_F32 && !u_inj && ind_out && !w_out &&
+                       (integrand == VF_INT_SYMGAUSS || integrand == VF_INT_BREIT_WIGNER);
+  const bool f32 = f32_tap || (precision == VF_PREC_F32 && integrand >= VF_INT_SYMGAUSS &&
+                               integrand <= VF_INT_SUM && !u_inj && !ind_out && !x_out && !w_out);
+  const void* k = jit       ? nullptr
+                  : f32_tap ? vf::plus_f32_tap_kernel(n_dim, integrand)
+                  : f32     ? vf::plus_f32_kernel(n_dim, integrand)
+                            : plus_kernel(precision, n_dim, integrand);
   if (!k && !jit) return err(VF_ERR_UNSUPPORTED, "vf_plus_sample: no kernel");
   vf::PlusArgs a;
   a.grid = grid;

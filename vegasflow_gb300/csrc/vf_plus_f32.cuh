@@ -29,7 +29,10 @@ __host__ __device__ inline int plus_f32_smem_bytes(int D, int train, int threads
   return D * VF_BINS * 8 + (train ? (threads / 32) * VF_PLUS_HIST_COPIES * D * VF_BINS * 4 : 0);
 }
 
-template <int D, int INTEG>
+// TAP: the parity instantiation, which also writes every event's bin indices
+// (a.ind_out, [n_events][D] int32) and point (a.x_out, float32, when not NULL)
+// in event order; the kernels of the hot path are TAP = false.
+template <int D, int INTEG, bool TAP = false>
 __global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel(const PlusArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NB = D * VF_BINS;
@@ -112,6 +115,13 @@ __global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel
             wf = (d == 0) ? c.y : wf * c.y;
             bins[d] = d * VF_BINS + (int)i;
           }
+        }
+      }
+      if constexpr (TAP) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          a.ind_out[e * D + d] = bins[d] - d * VF_BINS;
+          if (a.x_out) static_cast<float*>(a.x_out)[e * D + d] = x[d];
         }
       }
       float f;

@@ -133,8 +133,11 @@ __host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, 
 }
 
 // THREADS: the block size (an autotuner choice, 128 or 256); the register cap
-// (launch bounds) stays at 64 per thread for both.
-template <int D, int INTEG, int THREADS = VF_THREADS>
+// (launch bounds) stays at 64 per thread for both.  TAP: the parity
+// instantiation, which also writes every event's D bin indices to a.ind_out
+// ([n_events][D] int32); the kernels of the hot path are TAP = false, where the
+// writes do not exist.
+template <int D, int INTEG, int THREADS = VF_THREADS, bool TAP = false>
 __global__ void __launch_bounds__(THREADS, VF_F32_MIN_BLOCKS * VF_THREADS / THREADS)
 vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -266,6 +269,14 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
     return v2;
   };
 
+  // parity tap: the event's bin indices (bins[] holds d 50 + bin)
+  auto tap = [&](long long ev_idx, const int (&bins)[D]) {
+    if constexpr (TAP) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) a.ind_out[ev_idx * D + d] = bins[d] - d * VF_BINS;
+    }
+  };
+
   // one event's Philox words -> bins, weight and the Gaussian exponent (or x)
   auto draw = [&](u64 ev, int (&bins)[D], float& wf, float& s, float (&x)[D]) {
 #pragma unroll
@@ -311,6 +322,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
       if (have) {
         draw(ev, bins, wf, s, x);
         v2 = finish(bins, wf, s, x);
+        tap(e, bins);
       }
       const bool use = have && v2 >= 1.17549435e-38f && v2 <= 3.40282347e38f;  // normal, finite
       float l = use ? __log2f(v2) : 0.0f;
@@ -359,6 +371,8 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
         draw(ev1, b1, wf1, s1_, x1);
         finish(b0, wf0, s0, x0);
         finish(b1, wf1, s1_, x1);
+        tap(e, b0);
+        tap(e + stride, b1);
       }
     }
     for (; e < n; e += stride) {
@@ -369,11 +383,12 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
       draw(ev, bins, wf, s, x);
       const float v2 = finish(bins, wf, s, x);
       if (fixedp) add_fixed(bins, v2, ev);
+      tap(e, bins);
     }
   } else {
     // injected float64 uniforms, [n][D] row-major, streamed once
     int bad = 0;
-    auto injected_event = [&](const u64 (&ub)[D]) {
+    auto injected_event = [&](const u64 (&ub)[D], long long ev_idx) {
       int bins[D];
       float x[D];
       float wf = 1.0f, s = 0.0f;
@@ -403,6 +418,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
       const float v2 = finish(bins, wf, s, x);
       if (fixedp)  // injected uniforms: the float table, no scale
         for (int d = 0; d < D; ++d) atomicAdd(hovf + bins[d], v2);
+      tap(ev_idx, bins);
     };
     if (a.tma_swizzle != 0 && (D == 4 || D == 8 || D == 16)) {
       // Tiles of THREADS events (the grid-stride assignment: tile t holds
@@ -448,7 +464,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           tma_load_tile(stage, a.tmap, 0, (int)((t + G) * THREADS), bar, TILEB);
         }
-        if (t * THREADS + tid < n) injected_event(ub);
+        if (t * THREADS + tid < n) injected_event(ub, t * THREADS + tid);
       }
     } else {
       // plain loads: 16-byte (evict-first) when D is even and the array is
@@ -468,7 +484,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
 #pragma unroll
           for (int d = 0; d < D; ++d) ub[d] = (u64)__ldcs(up + d);
         }
-        injected_event(ub);
+        injected_event(ub, e);
       }
     }
     if (bad && a.flags) atomicOr(a.flags, VF_FLAG_INDEX_RANGE);
