@@ -288,6 +288,20 @@ int vf_consume_array_into_indices(const double* input, const int* indices, long 
                                   int result_size, double* out, int* flags, void* stream);
 
 /*
+ * The float64 uniforms that the fp32 samplers' integer maps stand for, for
+ * precision statements on identical events (no counterpart in the reference):
+ * u_out[e][d] = (word + 1/2) / 2^32 with `word` the Philox4x32-10 word d of
+ * event ev_offset + e -- counter (ev, ev >> 32, call_ctr << 4 | d / 4, word3),
+ * key `seed`.  word3 is call_ctr >> 28 for vf_sample (fp32 VEGAS) and
+ * vf_plus_sample (fp32 VEGAS+, events in iteration order), and the integral's
+ * stream id for vf_batch_sample.  Fed to the float64 samplers as injected
+ * uniforms, they reproduce the fp32 kernels' events in the reference's float64
+ * arithmetic.  u_out: device [n][n_dim].
+ */
+int vf_philox_uniforms(unsigned long long seed, unsigned int call_ctr, unsigned int word3, long long ev_offset,
+                       long long n, int n_dim, double* u_out, void* stream);
+
+/*
  * One VEGAS iteration (sample, reduce, sigma, and refinement of `grid` in place
  * when `train`) that allocates nothing.  No counterpart in the reference: it
  * serves callers that cannot call cudaMalloc -- plugins whose host framework

@@ -195,6 +195,16 @@ def grid_interchange(ref_inst):
 
 # -- C2 precision comparator: the reference in float64 and in its float32 mode
 C2P_N, C2P_ITERS, C2P_SEED = 10_000_000, 3, 11
+# Raw uniforms are floored at C2P_FLOOR in every run of the comparator: in the
+# reference's float32 mode a raw uniform below ~3e-8 gives u whose 1 - u rounds
+# to 1, so xn = 50 and the gather of the bin's upper edge (vflow.py:67-71) reads
+# index 51 of a 51-edge grid -- TensorFlow raises on the CPU.  At 1e7 x 8
+# uniforms per iteration about two such draws occur per iteration.
+C2P_FLOOR = 3e-8
+
+
+def c2_raw_source(rng):
+    return lambda shape: np.maximum(rng.random(shape), C2P_FLOOR)
 
 
 def c2_precision_child(out_path):
@@ -204,8 +214,7 @@ def c2_precision_child(out_path):
     raw uniforms of every iteration drawn from default_rng(C2P_SEED) in order."""
     from vegasflow.configflow import DTYPE
 
-    rng = np.random.default_rng(C2P_SEED)
-    tfshim.set_uniform_source(lambda shape: rng.random(shape))
+    tfshim.set_uniform_source(c2_raw_source(np.random.default_rng(C2P_SEED)))
 
     def gauss(xarr, weight=None):
         a = tf.constant(0.1, dtype=DTYPE)
@@ -229,7 +238,8 @@ def c2_precision():
     import subprocess
     import tempfile
 
-    out = {"n_events": np.int64(C2P_N), "iterations": np.int64(C2P_ITERS), "seed": np.int64(C2P_SEED)}
+    out = {"n_events": np.int64(C2P_N), "iterations": np.int64(C2P_ITERS), "seed": np.int64(C2P_SEED),
+           "raw_floor": np.float64(C2P_FLOOR)}
     with tempfile.TemporaryDirectory() as tmp:
         for bits in ("64", "32"):
             path = os.path.join(tmp, f"c2_{bits}.npz")

@@ -171,3 +171,14 @@ def test_plus_fp32_bins_are_the_reference_bins(n_dim, n_events, adaptive, which)
     np.testing.assert_array_equal(got, oracle.plus_bins_from_words(words, pts, inst._n_strat))
     # the points: float32 through the per-bin table, within 2e-6 of the float64 map
     assert np.max(np.abs(x.cpu().numpy().astype(np.float64) - x64)) < 2e-6
+
+
+@pytest.mark.parametrize("n_dim,call,offset", [(1, 0, 0), (8, 3, 5), (11, (1 << 28) + 2, 1 << 33)])
+def test_philox_uniforms_are_the_words_uniforms(n_dim, call, offset):
+    """vf_philox_uniforms writes u = (word + 1/2) / 2^32 of the samplers' words."""
+    n, seed = 100_000, 77
+    u = torch.empty((n, n_dim), dtype=torch.float64, device="cuda")
+    nat.call("vf_philox_uniforms", seed, call, call >> 28, offset, n, n_dim, nat.ptr(u), nat.stream_handle())
+    torch.cuda.synchronize()
+    want = oracle.uniforms_of_words(oracle.philox_words(seed, call, offset, n, n_dim))
+    np.testing.assert_array_equal(u.cpu().numpy(), want)

@@ -540,6 +540,22 @@ int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, in
   return check_launch("vf_refine_grid");
 }
 
+int vf_philox_uniforms(unsigned long long seed, unsigned int call_ctr, unsigned int word3, long long ev_offset,
+                       long long n, int n_dim, double* u_out, void* stream) {
+  if (!u_out && n > 0) return fail(VF_ERR_ARG, "vf_philox_uniforms: u_out is NULL");
+  if (n_dim < 1 || n_dim > VF_MAX_DIM) return fail(VF_ERR_UNSUPPORTED, "vf_philox_uniforms: n_dim=%d", n_dim);
+  if (n < 0 || ev_offset < 0) return fail(VF_ERR_ARG, "vf_philox_uniforms: negative count/offset");
+  if (n == 0) return VF_OK;
+  vf::SampleArgs a;
+  fill_philox(a, seed, call_ctr);
+  long long blocks = (n + 255) / 256;
+  const int cap = 8 * (sm_count() > 0 ? sm_count() : 1);
+  if (blocks > cap) blocks = cap;
+  vf::vf_philox_uniforms_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(a.rk, call_ctr << 4, word3, ev_offset,
+                                                                               n, n_dim, u_out);
+  return check_launch("vf_philox_uniforms");
+}
+
 int vf_consume_array_into_indices(const double* input, const int* indices, long long n,
                                   int result_size, double* out, int* flags, void* stream) {
   if (!out || result_size < 1) return fail(VF_ERR_ARG, "vf_consume_array_into_indices: bad output");

@@ -155,6 +155,25 @@ __global__ void __launch_bounds__(64) vf_refine_kernel(double* grid, const doubl
 
 // utils.py:17-44: out[b] = sum of input[e] with indices[e] == b.  `out` must be
 // zeroed.  Shared-memory bins, then one float64 atomic per bin per block.
+// The float64 uniforms u = (word + 1/2) / 2^32 that the fp32 samplers' integer
+// maps stand for (word d of event e: Philox4x32-10 block q = d / 4 of counter
+// (e, e >> 32, c2base | q, word3)), [n][n_dim] row-major.
+__global__ void __launch_bounds__(256) vf_philox_uniforms_kernel(RoundKeys rk, unsigned int c2base,
+                                                                 unsigned int word3, long long ev_offset,
+                                                                 long long n, int n_dim, double* __restrict__ u) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    const unsigned long long ev = (unsigned long long)(ev_offset + e);
+    for (int q = 0; 4 * q < n_dim; ++q) {
+      unsigned int c0 = (unsigned int)ev, c1 = (unsigned int)(ev >> 32), c2 = c2base | (unsigned int)q, c3 = word3;
+      philox4x32_10_rk(c0, c1, c2, c3, rk);
+      const unsigned int w[4] = {c0, c1, c2, c3};
+      for (int j = 0; j < 4 && 4 * q + j < n_dim; ++j)
+        u[e * n_dim + 4 * q + j] = ((double)w[j] + 0.5) * 2.3283064365386962890625e-10;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) vf_consume_kernel(const double* __restrict__ in,
                                                          const int* __restrict__ idx, long long n,
                                                          int size, double* out, int* flags) {

@@ -448,6 +448,7 @@ class VegasServer:
                 r.finished = r.arrival  # no clock: latencies are not measured
         served = [r for r in self.done if r.status in ("converged", "finished")]
         lat = [r.latency for r in served]
+        lat_conv = [r.latency for r in served if r.converged]
         flags = int(self._flags.item())
         by_status = {}
         for r in self.done:
@@ -456,6 +457,9 @@ class VegasServer:
                 "status": by_status,
                 "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99),
                 "mean_latency_s": float(np.mean(lat)) if lat else float("nan"),
+                # requests that reached their target sigma (the rest stopped at the iteration cap)
+                "p50_converged_s": percentile(lat_conv, 50), "p99_converged_s": percentile(lat_conv, 99),
+                "reached_target_fraction": len(lat_conv) / len(served) if served else float("nan"),
                 "events": self.events_done, "wall_s": wall, "busy_s": busy,
                 "events_per_s": self.events_done / wall if wall > 0 else float("nan"),
                 "steps": self.steps, "flags": flags}
