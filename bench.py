@@ -76,8 +76,10 @@ def _parse():
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--events", type=int, default=EVENTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serving-seconds", type=float, default=10.0,
-                    help="arrival window of the served Poisson stream (0 = skip; the full run is 60)")
+    ap.add_argument("--serving-seconds", type=float, default=60.0,
+                    help="arrival window of the served Poisson stream (0 = skip)")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the fp32-versus-float64 comparisons on identical events")
     ap.add_argument("--no-batched", action="store_true", help="skip the 1,024-integral batched run")
     ap.add_argument("--no-injected", action="store_true",
                     help="skip the injected-uniform (HBM-streaming) measurement")
@@ -263,6 +265,164 @@ def workload_config(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+def timed_iterations(dev, precision, n_events, K, W, seed, flush, world=1, n_dim=N_DIM):
+    """W warm-up + K timed iterations of the n_dim Gaussian (a = 0.1), each
+    bracketed by CUDA events on the launching stream with an L2 flush (a write
+    of ``flush``) before it; returns the integrator, per-iteration and sampler
+    times (s), the history rows and the running average."""
+    import numpy as np
+    import torch
+
+    from vegasflow_gb300 import VegasFlow, integrands
+
+    stream = torch.cuda.current_stream()
+    inst = VegasFlow(n_dim, n_events, verbose=False, precision=precision, seed=seed, device=dev)
+    inst.compile(integrands.symgauss(A_WIDTH))
+    for _ in range(W):
+        inst._run_iteration()
+    inst._reset_average()
+    torch.cuda.synchronize()
+    barrier(world)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    for k in range(K):
+        flush.fill_(float(k))
+        a, b, c = ev[k]
+        a.record(stream)
+        inst._fill_partials(train=inst.train)
+        b.record(stream)
+        inst._end_iteration(train=inst.train)
+        c.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    step_ms = [a.elapsed_time(c) for a, b, c in ev]
+    samp_ms = [a.elapsed_time(b) for a, b, c in ev]
+    hist = inst._workspace()["history"][:K].cpu().numpy()
+    avg = inst._workspace()["avg"].cpu().numpy()
+    return inst, np.array(step_ms) / 1e3, np.array(samp_ms) / 1e3, hist, avg
+
+
+def c2_small_run(dev, flush, K=10, W=3, n_events=10_000_000):
+    """C2's second size: the 8-D Gaussian at 1e7 events per iteration, fp32
+    fused and float64, timed as the headline (10 trained iterations)."""
+    exact = math.erf(0.5 / A_WIDTH) ** N_DIM
+    out = {"workload": f"8-D Gaussian a=0.1, {n_events:.0e} events/iteration, {K} trained iterations"}
+    for prec, seed in (("fp32", 12), ("fp64", 13)):
+        _, t, smp, _, avg = timed_iterations(dev, prec, n_events, K, W, seed, flush)
+        out[prec] = {"events_per_s": n_events * K / float(t.sum()), "ms_per_iteration": 1e3 * float(t.mean()),
+                     "sampler_ms": 1e3 * float(smp.mean()), "mean": float(avg[2]), "sigma": float(avg[3]),
+                     "pull_vs_exact": (float(avg[2]) - exact) / float(avg[3])}
+    out["fp32_over_fp64"] = out["fp32"]["events_per_s"] / out["fp64"]["events_per_s"]
+    return out
+
+
+def precision_run(dev):
+    """fp32 - float64 on identical events, in units of the float64 sigma, per
+    configuration.  The float64 side is this project's float64 GPU path (the
+    reference's arithmetic, bin for bin; the parity tests pin it to the
+    reference's own runs) fed the fp32 form's events: the uniforms its Philox
+    words stand for (vf_philox_uniforms), on the fp32 run's grid and event
+    layout of that iteration.  C2 compares on the reference's injected uniforms
+    instead, beside the reference's own float32 mode (its float64 and float32
+    runs recorded under the NumPy stand-in for TensorFlow in
+    tests/golden/c2_precision.npz)."""
+    import numpy as np
+    import torch
+
+    from vegasflow_gb300 import VegasFlow, VegasFlowPlus, integrands
+    from vegasflow_gb300 import _native as nat
+    from vegasflow_gb300.batch import VegasBatch, c4_specs
+
+    def own_uniforms(seed, call, word3, n, d):
+        u = torch.empty((n, d), dtype=torch.float64, device=dev)
+        nat.call("vf_philox_uniforms", seed, call, word3, 0, n, d, nat.ptr(u), nat.stream_handle())
+        return u
+
+    def summary(pulls):
+        p = np.asarray(pulls, dtype=np.float64)
+        return {"fp32_minus_fp64_over_sigma": [float(v) for v in p], "max_abs": float(np.max(np.abs(p)))}
+
+    out = {}
+    # C1: 4-D Gaussian, 1e6 events, 5 trained iterations
+    n, d, seed = 1_000_000, 4, 7
+    f32 = VegasFlow(d, n, verbose=False, precision="fp32", seed=seed, device=dev)
+    f32.compile(integrands.symgauss(A_WIDTH))
+    f64 = VegasFlow(d, n, verbose=False, precision="fp64", seed=seed, device=dev, events_limit=n)
+    f64.compile(integrands.symgauss(A_WIDTH))
+    pulls = []
+    for _ in range(5):
+        grid, call = f32.divisions.clone(), f32._call_ctr
+        r32, _ = f32._run_iteration()
+        f64.divisions.copy_(grid)
+        u = own_uniforms(seed, call, call >> 28, n, d)
+        f64.set_uniform_source(lambda m, dd, u=u: u)
+        r64, s64 = f64._run_iteration()
+        pulls.append((float(r32) - float(r64)) / float(s64))
+    out["C1"] = summary(pulls)
+    # C3: VegasFlowPlus adaptive, 6-D Breit-Wigner x linear, 2e6 events, 3 iterations
+    n, d, seed = 2_000_000, 6, 21
+    coeffs = np.random.default_rng(3).random(5)
+    p32 = VegasFlowPlus(d, n, adaptive=True, verbose=False, precision="fp32", seed=seed, device=dev)
+    p32.compile(integrands.breit_wigner(coeffs))
+    p64 = VegasFlowPlus(d, n, adaptive=True, verbose=False, precision="fp64", seed=seed, device=dev)
+    p64.compile(integrands.breit_wigner(coeffs))
+    pulls = []
+    for _ in range(3):
+        grid, n_ev, start = p32.divisions.clone(), p32.n_ev.clone(), p32._ev_start.clone()
+        n_tot, call = int(p32.n_events), p32._call_ctr
+        r32, _ = p32._run_iteration()
+        p64.divisions.copy_(grid)
+        p64.n_ev.copy_(n_ev)
+        p64._ev_start.copy_(start)
+        p64._n_events, p64._n_ev_stale = n_tot, False
+        u = own_uniforms(seed, call, call >> 28, n_tot, d)
+        p64.set_uniform_source(lambda m, dd, u=u: u)
+        r64, s64 = p64._run_iteration()
+        pulls.append((float(r32) - float(r64)) / float(s64))
+    out["C3"] = summary(pulls)
+    # C4: the first iteration of 16 resolvable batched integrals of at most 2e6 events
+    specs = c4_specs()
+    picks = [i for i, (dd, nn, f) in enumerate(specs)
+             if nn <= 2_000_000 and nn * np.prod(np.asarray(f.params(dd))[dd:] * np.sqrt(np.pi)) >= 100][:16]
+    b = VegasBatch([specs[i] for i in picks], seed=11, stream_ids=picks)
+    b.run(1)
+    first = b.history_host()[:, 0, :]
+    pulls = []
+    for k, i in enumerate(picks):
+        dd, nn, f = specs[i]
+        g64 = VegasFlow(dd, nn, verbose=False, precision="fp64", seed=11, device=dev, events_limit=nn)
+        g64.compile(f)
+        u = own_uniforms(11, 0, i, nn, dd)
+        g64.set_uniform_source(lambda m, ddd, u=u: u)
+        r64, s64 = g64._run_iteration()
+        pulls.append((float(first[k, 0]) - float(r64)) / float(s64))
+    out["C4"] = dict(summary(pulls), integrals=len(picks))
+    # C2 on the reference's injected uniforms: fused fp32, float64 path, reference float32 mode
+    fx = np.load(os.path.join(ROOT, "tests", "golden", "c2_precision.npz"))
+    n, iters, floor = int(fx["n_events"]), int(fx["iterations"]), float(fx["raw_floor"])
+    h64 = fx["f64/history"]
+    got = {}
+    for prec in ("fp32", "fp64"):
+        rng = np.random.default_rng(int(fx["seed"]))
+
+        def source(m, dd, rng=rng):
+            raw = np.maximum(rng.random((m, dd)), floor)
+            return torch.as_tensor(raw * ((1.0 - 1e-8) - 1e-8) + 1e-8, device=dev)
+
+        inst = VegasFlow(N_DIM, n, verbose=False, precision=prec, device=dev)
+        inst.compile(integrands.symgauss(A_WIDTH))
+        inst.set_uniform_source(source)
+        got[prec] = np.array([[float(v) for v in inst._run_iteration()] for _ in range(iters)])
+    out["C2"] = {"events": n, "iterations": iters,
+                 "fused_fp32_minus_reference_fp64_over_sigma": [float(v) for v in (got["fp32"][:, 0] - h64[:, 0])
+                                                                 / h64[:, 1]],
+                 "reference_fp32_mode_minus_fp64_over_sigma": [float(v) for v in (fx["f32/history"][:, 0]
+                                                                                   - h64[:, 0]) / h64[:, 1]],
+                 "gpu_fp64_minus_reference_fp64_relative": float(np.max(np.abs(got["fp64"][:, 0] - h64[:, 0])
+                                                                        / np.abs(h64[:, 0])))}
+    return out
+
+
 def main():
     args = _parse()
     rank, world, local = dist_setup(args.gpus)
@@ -294,33 +454,7 @@ def main():
         return
 
     def timed_run(precision, seed):
-        """W warm-up + K timed iterations; returns per-iteration and sampler times (s)."""
-        inst = VegasFlow(N_DIM, args.events, verbose=False, precision=precision, seed=seed, device=dev)
-        inst.compile(integrands.symgauss(A_WIDTH))
-        for _ in range(W):
-            inst._run_iteration()
-        inst._reset_average()
-        torch.cuda.synchronize()
-        barrier(world)
-        step_ms, samp_ms = [], []
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-               torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-        for k in range(K):
-            flush.fill_(float(k))
-            a, b, c = ev[k]
-            a.record(stream)
-            inst._fill_partials(train=inst.train)
-            b.record(stream)
-            inst._end_iteration(train=inst.train)
-            c.record(stream)
-        torch.cuda.synchronize()
-        barrier(world)
-        for a, b, c in ev:
-            step_ms.append(a.elapsed_time(c))
-            samp_ms.append(a.elapsed_time(b))
-        hist = inst._workspace()["history"][:K].cpu().numpy()
-        avg = inst._workspace()["avg"].cpu().numpy()
-        return inst, np.array(step_ms) / 1e3, np.array(samp_ms) / 1e3, hist, avg
+        return timed_iterations(dev, precision, args.events, K, W, seed, flush, world)
 
     with ClockSampler(local) as clocks:
         inst32, t32, s32, h32, a32 = timed_run("fp32", seed=2 + 1000 * rank)
@@ -349,6 +483,7 @@ def main():
         injected = None if args.no_injected else injected_run(dev, args.events, K, W)
         sampler = None if args.no_injected else sampler_run(dev, args.events, K, W)
         configs = None if args.no_batched else configs_run(dev)
+        c2_small = c2_small_run(dev, flush) if args.events == EVENTS and not args.no_batched else None
     clk = clocks.summary()
 
     total32 = float(t32.sum())
@@ -387,11 +522,14 @@ def main():
         "injected": injected,
         "sampler": sampler,
         "configs": configs,
+        "c2_1e7": c2_small,
         "gpu_launches": 2 * K,
         "clocks": clk,
     }
     if not args.no_batched:
         line["batched"] = batched_run(dev)
+    if not args.no_precision:
+        line["precision"] = precision_run(dev)
     if args.serving_seconds > 0:
         line["serving"] = serving_run(args.serving_seconds)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -599,10 +737,25 @@ def batched_run(dev, n_iter=5, fp64_sample=True):
     torch.cuda.synchronize()
     t = a.elapsed_time(c) / 1e3
     ev = b.total_events() * n_iter
+    # pulls against the exact integrals, over the integrals VEGAS can resolve at
+    # these sizes (>= 100 expected events in the peak on the initial grid)
+    from vegasflow_gb300.integrands import gauss_exact
+
+    mean, sigma, _, flags = b.results()
+    pulls = []
+    for i, (d, n, f) in enumerate(specs):
+        p = np.asarray(f.params(d))
+        if n * np.prod(p[d:] * np.sqrt(np.pi)) >= 100 and np.isfinite(mean[i]) and sigma[i] > 0:
+            pulls.append((mean[i] - gauss_exact(p[:d], p[d:])) / sigma[i])
+    pulls = np.asarray(pulls)
     out = {"workload": "1,024 Gaussians, dims 2-16, 1e4-1e7 events/iteration, own grids, 5 iterations",
            "integrals": len(specs), "events_per_iteration": b.total_events(),
            "fp32_batched_events_per_s": ev / t, "ms_per_iteration": 1e3 * t / n_iter,
-           "graph": True, "launches_per_iteration": 2}
+           "graph": True, "launches_per_iteration": 2,
+           "pulls_vs_exact": {"resolvable": int(pulls.size), "mean": float(pulls.mean()),
+                              "rms": float(np.sqrt(np.mean(pulls ** 2))),
+                              "within_3_sigma": float(np.mean(np.abs(pulls) < 3.0))},
+           "flags": int(flags)}
     if not fp64_sample:
         return out
     # float64 one by one, on every 16th integral (64 of them)

@@ -62,10 +62,10 @@ extern "C" {
 #define VF_INT_JIT_BASE 1000   /* ids returned by vf_jit_integrand               */
 
 /* ---- tunables (vf_tune_set / vf_tune_get) ---------------------------------- */
-#define VF_TUNE_F32_HIST_COPIES 1 /* fp32 VEGAS histogram: 0 = joint tables of dimension
-                                      pairs (default), 1|2|4 = per-dimension, copies per warp,
-                                      8 = joint tables in fixed point (integer atomics)     */
-#define VF_TUNE_F32_THREADS 2     /* fp32 VEGAS block size: 128 | 256 (default)              */
+#define VF_TUNE_F32_HIST_COPIES 1 /* fp32 VEGAS histogram layout: 0 = joint tables of
+                                      dimension pairs (the only layout)                     */
+#define VF_TUNE_F32_THREADS 2     /* fp32 VEGAS Philox sampler block size: 1024 (default) |
+                                      512                                                   */
 #define VF_TUNE_F32_BLOCKS_PER_SM 3 /* fp32 VEGAS persistent blocks per SM, 0 = all that fit
                                       (default); sets the events per thread                */
 

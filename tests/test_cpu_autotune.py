@@ -15,16 +15,18 @@ def test_launch_shape_validation():
     with pytest.raises(ValueError):
         autotune.LaunchShape(blocks_per_sm=17)
     with pytest.raises(ValueError):
-        autotune.LaunchShape(hist_copies=3)
-    s = autotune.LaunchShape(128, 2, 4)
+        autotune.LaunchShape(hist_copies=8)
+    with pytest.raises(ValueError):
+        autotune.LaunchShape(threads=256)
+    s = autotune.LaunchShape(512, 1, 0)
     assert autotune.LaunchShape.from_dict(s.as_dict()) == s
-    assert hash(s) == hash(autotune.LaunchShape(128, 2, 4))
+    assert hash(s) == hash(autotune.LaunchShape(512, 1, 0))
     assert s != autotune.DEFAULT_SHAPE
 
 
 def test_candidates_cover_the_space():
     train = autotune.candidates(train=True)
-    assert len(set(train)) == len(train) == 18
+    assert len(set(train)) == len(train) == 3
     assert autotune.DEFAULT_SHAPE in train
     frozen = autotune.candidates(train=False)
     assert {c.hist_copies for c in frozen} == {0}  # no histogram when the grid is frozen
@@ -44,9 +46,9 @@ def test_cache_round_trip(tmp_path):
     path = tmp_path / "sub" / "shapes.json"
     c = autotune.TuneCache(str(path))
     assert c.get("k") is None
-    c.put("k", autotune.LaunchShape(128, 1, 2), 0.5, 0.7)
+    c.put("k", autotune.LaunchShape(512, 1, 0), 0.5, 0.7)
     again = autotune.TuneCache(str(path))
-    assert again.get("k") == autotune.LaunchShape(128, 1, 2)
+    assert again.get("k") == autotune.LaunchShape(512, 1, 0)
     data = json.loads(path.read_text())
     assert data["k"]["ms"] == 0.5 and data["k"]["default_ms"] == 0.7
 
@@ -69,8 +71,9 @@ def test_cache_path_env(monkeypatch, tmp_path):
 def test_native_tunables_checked():
     lib = nat.load()
     v = ctypes.c_int(0)
-    for key, bad in ((nat.VF_TUNE_F32_THREADS, 64), (nat.VF_TUNE_F32_BLOCKS_PER_SM, -1),
-                     (nat.VF_TUNE_F32_BLOCKS_PER_SM, 17), (nat.VF_TUNE_F32_HIST_COPIES, 3), (99, 0)):
+    for key, bad in ((nat.VF_TUNE_F32_THREADS, 64), (nat.VF_TUNE_F32_THREADS, 256),
+                     (nat.VF_TUNE_F32_BLOCKS_PER_SM, -1), (nat.VF_TUNE_F32_BLOCKS_PER_SM, 17),
+                     (nat.VF_TUNE_F32_HIST_COPIES, 3), (nat.VF_TUNE_F32_HIST_COPIES, 8), (99, 0)):
         assert lib.vf_tune_get(key, ctypes.byref(v)) == (nat.VF_ERR_ARG if key == 99 else nat.VF_OK)
         before = v.value
         assert lib.vf_tune_set(key, bad) == nat.VF_ERR_ARG
@@ -78,8 +81,8 @@ def test_native_tunables_checked():
             assert lib.vf_tune_get(key, ctypes.byref(v)) == nat.VF_OK and v.value == before
     saved = autotune.current()
     try:
-        autotune.apply(autotune.LaunchShape(128, 3, 2))
-        assert autotune.current() == autotune.LaunchShape(128, 3, 2)
+        autotune.apply(autotune.LaunchShape(512, 3, 0))
+        assert autotune.current() == autotune.LaunchShape(512, 3, 0)
     finally:
         autotune.apply(saved)
 

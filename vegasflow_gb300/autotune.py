@@ -3,13 +3,15 @@
 The sampler's speed depends on three choices that do not change its results
 beyond float rounding (the Philox stream is indexed by event, not by thread):
 
-* ``threads``       -- block size, 128 or 256;
+* ``threads``       -- block size, 1024 or 512 (one or two resident blocks per
+  SM at 64 registers per thread);
 * ``blocks_per_sm`` -- persistent blocks per SM (0 = all that fit); with the
   block size it fixes how many events each thread walks, and the number of
   partial rows the iteration-end kernel reduces;
 * ``hist_copies``   -- histogram layout while training: 0 = joint tables of
-  dimension pairs, 1|2|4 = per-dimension tables with that many copies per warp,
-  8 = the joint tables in fixed point (integer atomics).
+  dimension pairs, the one layout the sampler has (the per-dimension and
+  fixed-point layouts measured slower with the replicated bin table and were
+  removed); kept as a field so cached shapes stay comparable.
 
 ``tune()`` times every candidate on the integrator's own workload (grid,
 integrand, event count) with CUDA events on the launching stream, keeps the
@@ -32,9 +34,9 @@ import torch
 
 from . import _native as nat
 
-HIST_CANDIDATES = (0, 8, 4)
-THREAD_CANDIDATES = (256, 128)
-BLOCKS_PER_SM_CANDIDATES = (0, 2, 1)
+HIST_CANDIDATES = (0,)
+THREAD_CANDIDATES = (1024, 512)
+BLOCKS_PER_SM_CANDIDATES = (0, 1)
 
 _lock = threading.Lock()
 
@@ -44,13 +46,13 @@ class LaunchShape:
 
     __slots__ = ("threads", "blocks_per_sm", "hist_copies")
 
-    def __init__(self, threads=256, blocks_per_sm=0, hist_copies=0):
-        if threads not in (128, 256):
-            raise ValueError(f"threads must be 128 or 256, not {threads}")
+    def __init__(self, threads=1024, blocks_per_sm=0, hist_copies=0):
+        if threads not in (512, 1024):
+            raise ValueError(f"threads must be 512 or 1024, not {threads}")
         if not 0 <= blocks_per_sm <= 16:
             raise ValueError(f"blocks_per_sm must be in 0..16, not {blocks_per_sm}")
-        if hist_copies not in (0, 1, 2, 4, 8):
-            raise ValueError(f"hist_copies must be 0, 1, 2, 4 or 8, not {hist_copies}")
+        if hist_copies != 0:
+            raise ValueError(f"hist_copies must be 0 (joint pair tables), not {hist_copies}")
         self.threads = int(threads)
         self.blocks_per_sm = int(blocks_per_sm)
         self.hist_copies = int(hist_copies)
@@ -108,9 +110,11 @@ def current():
 
 
 def candidates(train=True):
-    """Every launch shape to try; the histogram layout only matters while training."""
+    """Every launch shape to try (a 1024-thread block is alone on its SM, so
+    ``blocks_per_sm`` only varies for 512-thread blocks)."""
     hists = HIST_CANDIDATES if train else (0,)
-    return [LaunchShape(t, b, h) for h in hists for t in THREAD_CANDIDATES for b in BLOCKS_PER_SM_CANDIDATES]
+    return [LaunchShape(t, b, h) for h in hists for t in THREAD_CANDIDATES for b in BLOCKS_PER_SM_CANDIDATES
+            if not (t == 1024 and b != 0)]
 
 
 def events_bucket(n_events):

@@ -40,8 +40,30 @@ def cuda_home():
     return os.path.dirname(os.path.dirname(os.path.realpath(nvcc_path())))
 
 
+# Sources compiled more than once, with per-variant defines (instantiation
+# units split by block size and dimension range so they build in parallel).
+VARIANTS = {
+    "vf_vegas_f32_inst.cu": [
+        (f"t{t}_{lo}_{hi}", [f"-DVF_INST_THREADS={t}", f"-DVF_INST_DLO={lo}", f"-DVF_INST_DHI={hi}"])
+        for t, lo, hi in ((1024, 1, 4), (1024, 5, 8), (1024, 9, 12), (1024, 13, 16), (512, 1, 8), (512, 9, 16))],
+    "vf_vegas_f32_inj.cu": [
+        (f"d{lo}_{hi}", [f"-DVF_INST_DLO={lo}", f"-DVF_INST_DHI={hi}"]) for lo, hi in ((1, 8), (9, 16))],
+}
+
+
 def _sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+
+
+def _units():
+    """(source, object, extra flags) for every object of the library."""
+    out = []
+    for s in _sources():
+        stem = os.path.splitext(os.path.basename(s))[0]
+        for tag, flags in VARIANTS.get(os.path.basename(s), [(None, [])]):
+            name = f"{stem}_{tag}" if tag else stem
+            out.append((s, os.path.join(BUILD, name + ".o"), flags))
+    return out
 
 
 def _headers():
@@ -94,18 +116,16 @@ def build(force=False, verbose=False, jobs=None, extra_flags=()):
     """Compile and link libvegasgb.so; returns its path."""
     os.makedirs(BUILD, exist_ok=True)
     write_jit_sources()
-    srcs = _sources()
     hdr_time = _newest(_headers())
     todo = []
-    objs = []
-    for s in srcs:
-        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(s))[0] + ".o")
+    objs = []  # only the current units' objects are linked (stale ones are ignored)
+    for s, obj, flags in _units():
         objs.append(obj)
         if force or not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(s), hdr_time):
-            todo.append((s, obj))
+            todo.append((s, obj, flags))
     jobs = jobs or min(len(todo) or 1, os.cpu_count() or 4)
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        list(ex.map(lambda so: _compile(so[0], so[1], verbose, list(extra_flags)), todo))
+        list(ex.map(lambda t: _compile(t[0], t[1], verbose, list(t[2]) + list(extra_flags)), todo))
     if force or todo or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
         home = cuda_home()
         lib64 = os.path.join(home, "lib64")

@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <cstdio>
 #include <cstring>
@@ -18,11 +19,11 @@
 
 namespace {
 
-// Tunables (vf_tune_set): histogram copies per warp of the fp32 VEGAS sampler.
-// 0 = joint pair tables, 1|2|4 = per-dimension tables with that many copies per warp.
+// Tunables (vf_tune_set): the histogram layout of the fp32 VEGAS sampler (0 =
+// joint pair tables, the only layout)
 std::atomic<int> g_f32_hist_copies{0};
-// block size of the fp32 VEGAS sampler (128 | 256)
-std::atomic<int> g_f32_threads{256};
+// block size of the fp32 VEGAS Philox sampler (1024 | 512)
+std::atomic<int> g_f32_threads{1024};
 // persistent blocks per SM of the fp32 VEGAS sampler (0 = as many as fit): with
 // the block size it sets the events each thread processes
 std::atomic<int> g_f32_blocks_per_sm{0};
@@ -142,6 +143,29 @@ int prepare_smem(const void* kernel, int smem) {
   return VF_OK;
 }
 
+// Blocks of `kernel` resident on the device at once (SMs x blocks per SM),
+// cached per (device, kernel, block size, shared memory): launches make no
+// occupancy query after the first.  0 on error.
+int resident_blocks(const void* kernel, int threads, int smem) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  static std::mutex mu;
+  static std::map<std::tuple<int, const void*, int, int>, int> cache;
+  const auto key = std::make_tuple(dev, kernel, threads, smem);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+    return 0;
+  const int fit = per_sm * sm_count();
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = fit;
+  return fit;
+}
+
 }  // namespace
 
 namespace vf {
@@ -156,7 +180,7 @@ int vf_version(void) { return 1; }
 
 int vf_tune_set(int key, int value) {
   if (key == VF_TUNE_F32_THREADS) {
-    if (value != 128 && value != 256) return fail(VF_ERR_ARG, "vf_tune_set: threads must be 128 or 256");
+    if (value != 512 && value != 1024) return fail(VF_ERR_ARG, "vf_tune_set: threads must be 512 or 1024");
     g_f32_threads.store(value);
     return VF_OK;
   }
@@ -166,8 +190,7 @@ int vf_tune_set(int key, int value) {
     return VF_OK;
   }
   if (key == VF_TUNE_F32_HIST_COPIES) {
-    if (value != 0 && value != 1 && value != 2 && value != 4 && value != VF_F32_HIST_FIXED)
-      return fail(VF_ERR_ARG, "vf_tune_set: histogram layout must be 0 (joint pairs), 1, 2, 4 or 8 (fixed point)");
+    if (value != 0) return fail(VF_ERR_ARG, "vf_tune_set: the histogram layout must be 0 (joint pair tables)");
     g_f32_hist_copies.store(value);
     return VF_OK;
   }
@@ -209,11 +232,17 @@ int vf_preload(void) {
   auto load = [&](const void* k) {
     if (k && e == cudaSuccess) e = cudaFuncGetAttributes(&attr, k);
   };
-  for (int d = 1; d <= VF_MAX_DIM; ++d)
+  for (int d = 1; d <= VF_MAX_DIM; ++d) {
     for (int integ = VF_INT_SYMGAUSS; integ <= VF_INT_SUM; ++integ) {
-      load(vf::vegas_f32_kernel(d, integ, 256));
-      load(vf::vegas_f32_kernel(d, integ, 128));
+      load(vf::vegas_f32_kernel(d, integ, 1024));
+      load(vf::vegas_f32_kernel(d, integ, 512));
+      load(vf::vegas_f32_inj_kernel(d, integ, false));
     }
+    for (int integ : {VF_INT_SYMGAUSS, VF_INT_PROD}) {
+      load(vf::vegas_f32_tap_kernel(d, integ));
+      load(vf::vegas_f32_inj_kernel(d, integ, true));
+    }
+  }
   for (int d = 1; d <= VF_MAX_DIM; ++d) load(vf::vegas_f32_map_kernel(d));
   for (int dmax : {4, 8, 16})
     for (int integ = VF_INT_NONE; integ <= VF_INT_SUM; ++integ) {
@@ -257,7 +286,7 @@ int vf_sample_rows(int alg, int precision, int n_dim, int integrand, int train, 
   if (fast) {
     threads = g_f32_threads.load();
     k = vf::vegas_f32_kernel(n_dim, integ, threads);
-    smem = vf::vegas_f32_smem_bytes(n_dim, g_f32_hist_copies.load(), train, threads);
+    smem = vf::vegas_f32_smem_bytes(n_dim, train);
   } else {
     k = sample_kernel(precision, n_dim, integ);
     const int real = precision == VF_PREC_F64 ? 8 : 4;
@@ -314,8 +343,12 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
   // the fp32 VEGAS map alone (no integrand, Philox uniforms): x, w, indices to HBM
   const bool map_only = !jit && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS && integrand == VF_INT_NONE &&
                         !u_inj && !f_out && (x_out || w_out || ind_out);
-  const int threads = tap_fast ? 256 : (fast ? g_f32_threads.load() : VF_THREADS);
+  // fp32 VEGAS with a built-in integrand: the Philox kernel, or for injected
+  // uniforms the TMA-staged kernel (VF_INJ_THREADS per block)
+  const bool inj = fast && u_inj != nullptr;
+  const int threads = inj ? VF_INJ_THREADS : (tap_fast ? 1024 : (fast ? g_f32_threads.load() : VF_THREADS));
   const void* k = jit        ? nullptr
+                  : inj      ? vf::vegas_f32_inj_kernel(n_dim, integrand, tap_fast)
                   : tap_fast ? vf::vegas_f32_tap_kernel(n_dim, integrand)
                   : fast     ? vf::vegas_f32_kernel(n_dim, integrand, threads)
                              : sample_kernel(precision, n_dim, integrand);
@@ -369,7 +402,7 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
     if (taps && precision == VF_PREC_F32 && alg == VF_ALG_VEGAS)
       return fail(VF_ERR_UNSUPPORTED, "vf_sample: a JIT fp32 VEGAS integrand has no per-event taps");
     int fast_jit = 0;
-    a.hist_copies = g_f32_hist_copies.load();
+    a.hist_copies = 0;
     const int rc = vf::jit_launch(integrand, alg, precision, n_dim, &a, rows, a.train, stream, &fast_jit,
                                   &a.hist_copies);
     (void)fast_jit;
@@ -378,24 +411,23 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
   int smem;
   int blocks = rows;
   if (fast) {
-    a.hist_copies = g_f32_hist_copies.load();
-    smem = vf::vegas_f32_smem_bytes(n_dim, a.hist_copies, a.train, threads);
-    if (u_inj) {
-      // injected uniforms through TMA: one stage of `threads` rows, 1024-byte
-      // aligned; the grid is capped at the blocks that fit at once (the kernel
-      // clears the rows it does not own)
-      a.tma_swizzle = encode_uniform_tiles(a, u_inj, n_events, n_dim, threads);
-      if (a.tma_swizzle) {
-        smem += threads * 8 * n_dim + 1024;
-        int rc = prepare_smem(k, smem);
-        if (rc) return rc;
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem) != cudaSuccess || per_sm < 1)
-          return fail(VF_ERR_CUDA, "vf_sample: occupancy query for the TMA path failed");
-        const int fit = per_sm * sm_count();
-        if (fit < blocks) blocks = fit;
-      }
+    a.hist_copies = 0;
+    if (inj) {
+      // injected uniforms: TMA tiles of VF_INJ_ROWS rows into each group's
+      // stage ring when the array allows it
+      a.tma_swizzle = encode_uniform_tiles(a, u_inj, n_events, n_dim, VF_INJ_ROWS);
+      smem = vf::vegas_f32_inj_smem_bytes(n_dim, a.train, a.tma_swizzle != 0);
+    } else {
+      smem = vf::vegas_f32_smem_bytes(n_dim, a.train);
     }
+    // the grid is capped at the blocks resident at once: fewer than the
+    // caller's rows when they were counted for another shape (the kernel clears
+    // the rows it does not own)
+    int rc = prepare_smem(k, smem);
+    if (rc) return rc;
+    const int fit = resident_blocks(k, threads, smem);
+    if (fit < 1) return fail(VF_ERR_CUDA, "vf_sample: occupancy query for the fp32 sampler failed");
+    if (fit < blocks) blocks = fit;
   } else {
     a.hist_copies = hist_copies_for(precision);
     const int real = precision == VF_PREC_F64 ? 8 : 4;

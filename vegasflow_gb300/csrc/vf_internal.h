@@ -10,19 +10,34 @@ namespace vf {
 const void* sample_kernel_f64(int dmax, int integrand);
 const void* sample_kernel_f32(int dmax, int integrand);
 
-// The fp32 VEGAS sampler specialised on the exact dimension count (1..8 in
-// part a, 9..16 in part b) and the block size (128 or 256 threads).
-const void* vegas_f32_kernel_a256(int n_dim, int integrand);
-const void* vegas_f32_kernel_b256(int n_dim, int integrand);
-const void* vegas_f32_kernel_a128(int n_dim, int integrand);
-const void* vegas_f32_kernel_b128(int n_dim, int integrand);
-inline const void* vegas_f32_kernel(int n_dim, int integrand, int threads = 256) {
-  if (threads == 128)
-    return n_dim <= 8 ? vegas_f32_kernel_a128(n_dim, integrand) : vegas_f32_kernel_b128(n_dim, integrand);
-  return n_dim <= 8 ? vegas_f32_kernel_a256(n_dim, integrand) : vegas_f32_kernel_b256(n_dim, integrand);
+// The fp32 VEGAS Philox sampler specialised on the exact dimension count and
+// the block size (1024 or 512 threads), one function per instantiation unit.
+const void* vegas_f32_kernel_t1024_1_4(int n_dim, int integrand);
+const void* vegas_f32_kernel_t1024_5_8(int n_dim, int integrand);
+const void* vegas_f32_kernel_t1024_9_12(int n_dim, int integrand);
+const void* vegas_f32_kernel_t1024_13_16(int n_dim, int integrand);
+const void* vegas_f32_kernel_t512_1_8(int n_dim, int integrand);
+const void* vegas_f32_kernel_t512_9_16(int n_dim, int integrand);
+inline const void* vegas_f32_kernel(int n_dim, int integrand, int threads) {
+  if (threads == 512) return n_dim <= 8 ? vegas_f32_kernel_t512_1_8(n_dim, integrand)
+                                        : vegas_f32_kernel_t512_9_16(n_dim, integrand);
+  if (threads != 1024) return nullptr;
+  if (n_dim <= 4) return vegas_f32_kernel_t1024_1_4(n_dim, integrand);
+  if (n_dim <= 8) return vegas_f32_kernel_t1024_5_8(n_dim, integrand);
+  if (n_dim <= 12) return vegas_f32_kernel_t1024_9_12(n_dim, integrand);
+  return vegas_f32_kernel_t1024_13_16(n_dim, integrand);
 }
 
-// The parity instantiation of the fp32 VEGAS sampler (256 threads; writes each
+// The fp32 VEGAS sampler for injected float64 uniforms (VF_INJ_THREADS per block);
+// `tap`: its parity instantiation (VF_INT_SYMGAUSS and VF_INT_PROD only).
+const void* vegas_f32_inj_kernel_d1_8(int n_dim, int integrand, bool tap);
+const void* vegas_f32_inj_kernel_d9_16(int n_dim, int integrand, bool tap);
+inline const void* vegas_f32_inj_kernel(int n_dim, int integrand, bool tap) {
+  return n_dim <= 8 ? vegas_f32_inj_kernel_d1_8(n_dim, integrand, tap)
+                    : vegas_f32_inj_kernel_d9_16(n_dim, integrand, tap);
+}
+
+// The parity instantiation of the fp32 VEGAS Philox sampler (1024 threads; writes each
 // event's bin indices): VF_INT_SYMGAUSS and VF_INT_PROD, dimensions 1..16.
 const void* vegas_f32_tap_kernel(int n_dim, int integrand);
 

@@ -62,8 +62,10 @@ const Driver& driver() {
 
 struct JitKernel {
   CUmodule module = nullptr;
-  CUfunction fn = nullptr;       // the sampler (VEGAS+: the float64 / tap-writing one)
-  CUfunction fn_fast = nullptr;  // VEGAS+ in fp32: the float32 sampler for Philox uniforms
+  CUfunction fn = nullptr;       // the sampler (VEGAS+: the float64 / tap-writing one; fp32 VEGAS: the
+                                 // Philox kernel, 1024 threads per block)
+  CUfunction fn_fast = nullptr;  // VEGAS+ in fp32: the float32 sampler for Philox uniforms; fp32 VEGAS:
+                                 // the kernel for injected uniforms (1024 threads per block)
   int alg = 0, precision = 0, n_dim = 0, fast = 0, smem_set = 0, smem_set_fast = 0;
 };
 
@@ -100,7 +102,8 @@ std::string program_text(const char* source, const char* func_name, int alg, int
     }
   } else if (fast) {
     src += "#include \"vf_vegas_f32.cuh\"\n";
-    exprs->push_back("vf::vf_vegas_f32_kernel<" + std::to_string(n_dim) + ", 99>");
+    exprs->push_back("vf::vf_vegas_f32_kernel<" + std::to_string(n_dim) + ", 99, 1024>");
+    exprs->push_back("vf::vf_vegas_f32_inj_kernel<" + std::to_string(n_dim) + ", 99>");
   } else {
     src += "#include \"vf_sample.cuh\"\n";
     exprs->push_back(std::string("vf::vf_sample_kernel<") + real + ", " + std::to_string(vf::dim_bucket(n_dim)) +
@@ -232,8 +235,21 @@ int jit_launch(int integrand_id, int alg, int precision, int n_dim, void* args, 
     return set_error(VF_ERR_ARG, "JIT integrand was compiled for another algorithm, precision or n_dim");
   *fast_out = k.fast;
   int smem;
+  unsigned threads = VF_THREADS;
+  int blocks = rows;
+  // fp32 VEGAS: the injected-uniform kernel when uniforms are injected
+  const bool inj = k.fast && static_cast<const SampleArgs*>(args)->u_inj != nullptr;
+  const CUfunction fn = inj ? k.fn_fast : k.fn;
   if (k.fast) {
-    smem = vegas_f32_smem_bytes(n_dim, *hist_copies_inout, train);
+    // both fp32 VEGAS kernels run 1024-thread blocks, one per SM (64 registers
+    // per thread); the kernel clears the caller's rows beyond its grid
+    *hist_copies_inout = 0;
+    smem = inj ? vegas_f32_inj_smem_bytes(n_dim, train) : vegas_f32_smem_bytes(n_dim, train);
+    threads = 1024;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0 && sms < blocks)
+      blocks = sms;
   } else {
     *hist_copies_inout = precision == VF_PREC_F32 ? 8 : 1;
     smem = sample_smem_bytes(precision == VF_PREC_F64 ? 8 : 4, n_dim, *hist_copies_inout,
@@ -241,16 +257,18 @@ int jit_launch(int integrand_id, int alg, int precision, int n_dim, void* args, 
   }
   const Driver& drv = driver();
   if (!drv.ok) return set_error(VF_ERR_CUDA, "CUDA driver entry points unavailable");
-  if (smem > 48 * 1024 && k.smem_set < smem) {  // once per size: no attribute call in later (captured) launches
-    if (drv.func_set_attribute(k.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS)
+  const int have = inj ? k.smem_set_fast : k.smem_set;
+  if (smem > 48 * 1024 && have < smem) {  // once per size: no attribute call in later (captured) launches
+    if (drv.func_set_attribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS)
       return set_error(VF_ERR_CUDA, "cuFuncSetAttribute for a JIT kernel failed");
     std::lock_guard<std::mutex> lock(g_mu);
     JitKernel& kk = g_kernels[integrand_id - VF_INT_JIT_BASE];
-    if (kk.smem_set < smem) kk.smem_set = smem;
+    int& set = inj ? kk.smem_set_fast : kk.smem_set;
+    if (set < smem) set = smem;
   }
   void* params[] = {args};
   const CUresult r =
-      drv.launch_kernel(k.fn, rows, 1, 1, VF_THREADS, 1, 1, smem, (CUstream)stream, params, nullptr);
+      drv.launch_kernel(fn, blocks, 1, 1, threads, 1, 1, smem, (CUstream)stream, params, nullptr);
   if (r != CUDA_SUCCESS) return set_error(VF_ERR_LAUNCH, "cuLaunchKernel failed for a JIT kernel");
   return VF_OK;
 }

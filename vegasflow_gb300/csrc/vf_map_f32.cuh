@@ -24,7 +24,7 @@ namespace vf {
 
 // resident blocks per SM the register allocation is sized for (256 threads)
 #ifndef VF_MAP_MIN_BLOCKS
-#define VF_MAP_MIN_BLOCKS VF_F32_MIN_BLOCKS
+#define VF_MAP_MIN_BLOCKS 4
 #endif
 
 // One event's row of D 32-bit words into the staging tile in 16-byte stores (D a

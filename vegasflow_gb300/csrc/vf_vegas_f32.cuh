@@ -1,49 +1,61 @@
-// The fused fp32 VEGAS sampler: the performance path of the float32 form.
+// The fused fp32 VEGAS samplers: the performance path of the float32 form.
 //
-// Compared with the generic sampler (vf_sample.cuh) this kernel is specialised
-// at compile time on the exact dimension count and the integrand, draws the
-// Philox words with round keys held in the parameter block, and stages a
-// per-bin table that folds the importance map, the integration limits and --
-// for the Gaussian family -- the integrand's affine argument into one fused
-// multiply-add per dimension:
+// Two kernels, both specialised at compile time on the exact dimension count
+// and the integrand, reading nothing per event from HBM but their inputs:
 //
-//   bin i, fraction m in [1, 2) from p = 50 * ~word + 25 (exact, 64-bit):
-//       i = p >> 32,  m = 1 + (p mod 2^32) / 2^32  (23 bits)
-//   table cell {c0, c1} per (dimension, bin), computed in float64 and rounded once:
-//       generic integrand:  x  = c0 + c1 m,  c0 = xmin + (lo - delta) xdelta, c1 = delta xdelta
-//       Gaussian family:    t  = c0 + c1 m,  t = (x - mu) sqrt(log2 e) / a,
-//                           f  = 2^(-sum t^2)  (the normalisation goes to the float64 scale)
-//   weight w = prod_d c1 (float32); the constant 50^D * xjac (* pref / prod k) is
+//   vf_vegas_f32_kernel      in-kernel Philox4x32-10 uniforms (the benchmarked
+//                            path, C2's fp32 form)
+//   vf_vegas_f32_inj_kernel  injected float64 uniforms streamed from HBM by TMA
+//                            tiles (C2's injected mode)
+//
+// Per event and dimension one fused multiply-add through a per-bin table
+// {C0, C1} staged in shared memory, which folds the importance map, the
+// integration limits and -- for the Gaussian family -- the integrand's affine
+// argument:
+//
+//   generic integrand:  x = c0 + c1 (1 + frac),  c0 = xmin + (lo - delta) xdelta,
+//                       c1 = delta xdelta  (frac: the reference's fractional bin
+//                       coordinate, vflow.py:75-76)
+//   Gaussian family:    t = (x - mu) sqrt(log2 e) / a as the same affine map,
+//                       f = 2^(-sum t^2)  (the normalisation goes to the float64
+//                       scale)
+//   weight w = prod_d c1 (float32); the constant 50^D xjac (* pref / prod k) is
 //   applied in float64 to the block partials.
 //
-// Per event: accumulation of w f and (w f)^2 in TwoSum-compensated fp32, and
-// (when training) the (w f)^2 histogram in shared memory, in one of three
-// layouts (`hist_copies`; which is fastest depends on the dimension count and
-// the spread of the weights, so the launch-shape autotuner chooses):
-//   0      joint pairs (the default): dimensions (0,1), (2,3), ... share one
-//          50 x 50 table per block, so an event makes ceil(D/2) float atomic
-//          additions instead of D, and with 2500 cells the lanes of a warp rarely
-//          collide on an address.  At the end each dimension's 50 bins are the
-//          row or column sums of its pair's table (an odd last dimension keeps a
-//          plain 50-bin table).
-//   1,2,4  per-dimension tables, that many copies per warp (lane groups).
-//   8      fixed point (VF_F32_HIST_FIXED): the joint pair tables of layout 0
-//          as 32-bit integers, updated with native integer shared atomics (no
-//          result read back) instead of float atomics, which the hardware runs
-//          as compare-and-swap loops.  An event adds q = floor(S (w f)^2 + r),
-//          r a per-event dither in [0, 1) (a Weyl sequence of the event number),
-//          so the expectation of q / S is exact.  A cell cannot wrap: q is
-//          capped at Qmax = (2^32 - 1) / (events the block walks), and an event
-//          at or above the cap goes to a per-dimension float table instead.
-//          Each block picks its power-of-two scale S from the first event of
-//          every thread (S (w f)^2 about Qmax / 512 at their geometric mean);
-//          a block whose first events are all zero uses the float table only.
-//          The integer sums do not depend on the order of the atomics.
+// Philox kernel.  A word w stands for the uniform u = (w + 1/2) / 2^32, whose
+// reference bin is trunc(50 (1 - u)) (vflow.py:117, :67).  p = 50 w + 25 is
+// 50 u 2^32 exactly (64-bit), so j = p >> 32 = floor(50 u) and the reference bin
+// is 49 - j (50 u is never an integer); its fraction 1 - frac(50 u) comes from
+// p's low word.  The table is therefore stored in reversed bin order, cell j
+// holding bin 49 - j as C0 = c0 + 3 c1, C1 = -c1 (computed in float64, rounded
+// once), so that with m = 1 + (the top 23 bits of p mod 2^32) / 2^23 in [1, 2):
+//       C0 + C1 m = c0 + c1 (2 - frac(50 u)) = c0 + c1 (1 + frac(50 (1 - u)))
+// -- one 64-bit multiply-add, two bit operations and one table lookup per
+// dimension, no complement.  The weight's sign (-1)^D goes to the float64 scale.
+//
+// The table is replicated VF_F32_TC = 16 times, copy c in bank pair c: lane l
+// reads copy l % 16, so the 64-bit lookups of a half-warp never share a bank
+// (2 shared-memory wavefronts per warp lookup instead of ~7 with one copy; the
+// shared-memory pipe is what the histogram atomics compete for).
+//
+// Per event: TwoSum-compensated fp32 sums of w f and (w f)^2, and (when
+// training) the (w f)^2 histogram in joint tables of dimension pairs: dims
+// (0,1), (2,3), ... share one table of 50 rows per block, so an event makes
+// ceil(D/2) float atomic additions (compare-and-swap loops on this part)
+// instead of D.  Rows are VF_F32_JOINT_ROW floats: 64 with the column index
+// XOR-swizzled by the row's low bits (the cell address is shifts and a logical
+// operation, and a warp's random cells spread evenly over the banks), or 50.
+// At the end each dimension's 50 bins are its pair table's row or column sums
+// (an odd last dimension has a plain 50-bin table).
 #pragma once
 #include "vf_sample.cuh"
 
-#ifndef VF_F32_MIN_BLOCKS
-#define VF_F32_MIN_BLOCKS 4
+// lane-replicated copies of the per-bin table (Philox kernel)
+#define VF_F32_TC 16
+
+// floats per row of a joint pair table (64: XOR-swizzled columns; 50: plain)
+#ifndef VF_F32_JOINT_ROW
+#define VF_F32_JOINT_ROW 64
 #endif
 
 namespace vf {
@@ -54,7 +66,29 @@ __device__ __forceinline__ float ex2_approx_ftz(float x) {
   return y;
 }
 
+// floats of the 50 x 50 joint tables (plus a plain table for an odd last
+// dimension) with 50-float rows: the batched sampler and the injected kernel
 __host__ __device__ inline int vegas_f32_joint_floats(int D) { return (D / 2) * 2500 + (D & 1) * 50; }
+
+// The Philox kernel's joint tables: rows of VF_F32_JOINT_ROW floats.
+__host__ __device__ constexpr int vegas_f32_pair_floats() { return VF_BINS * VF_F32_JOINT_ROW; }
+__host__ __device__ inline int vegas_f32_hist_floats(int D) {
+  return (D / 2) * vegas_f32_pair_floats() + (D & 1) * VF_BINS;
+}
+__host__ __device__ inline int vegas_f32_table_bytes(int D) { return D * VF_BINS * VF_F32_TC * 8; }
+
+// Dynamic shared memory of the Philox kernel.
+__host__ __device__ inline int vegas_f32_smem_bytes(int D, int train) {
+  return vegas_f32_table_bytes(D) + (train ? vegas_f32_hist_floats(D) * 4 : 0);
+}
+
+// Offset of cell (row r, column c) of a joint pair table.
+__device__ __forceinline__ int joint_cell(int r, int c) {
+  if (VF_F32_JOINT_ROW == 64)
+    return (r << 6) + (c ^ (r & 31));
+  else
+    return r * VF_F32_JOINT_ROW + c;
+}
 
 // The reference's bin of an injected float64 uniform u, ind = trunc(fl(50 *
 // fl(1 - u))) (vflow.py:117, :67), without float64 arithmetic: for u in
@@ -83,7 +117,7 @@ __device__ __forceinline__ bool inj_bin_exact(u64 bits, int& ind, float& m) {
   return true;
 }
 
-// ---- TMA staging of injected uniforms (tiles of THREADS events x D float64)
+// ---- TMA staging of injected uniforms
 __device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(u32 bar, u32 count) {
@@ -116,128 +150,128 @@ __device__ __forceinline__ bool mbar_wait_bounded(u32 bar, u32 parity, int polls
   return false;
 }
 
-// the fixed-point histogram layout (hist_copies value)
-#define VF_F32_HIST_FIXED 8
+// ---- per-block constants and the per-bin table, shared by both kernels
 
-__host__ __device__ inline int vegas_f32_smem_bytes(int D, int copies_per_warp, int train,
-                                                    int threads = VF_THREADS) {
-  const int nb = D * VF_BINS;
-  int hist;
-  if (copies_per_warp == 0)
-    hist = vegas_f32_joint_floats(D) * 4;
-  else if (copies_per_warp == VF_F32_HIST_FIXED)
-    hist = (vegas_f32_joint_floats(D) + nb) * 4;  // integer joint tables, float overflow table
-  else
-    hist = (threads / 32) * copies_per_warp * nb * 4;
-  return nb * 8 + (train ? hist : 0);
-}
-
-// THREADS: the block size (an autotuner choice, 128 or 256); the register cap
-// (launch bounds) stays at 64 per thread for both.  TAP: the parity
-// instantiation, which also writes every event's D bin indices to a.ind_out
-// ([n_events][D] int32); the kernels of the hot path are TAP = false, where the
-// writes do not exist.
-template <int D, int INTEG, int THREADS = VF_THREADS, bool TAP = false>
-__global__ void __launch_bounds__(THREADS, VF_F32_MIN_BLOCKS * VF_THREADS / THREADS)
-vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  constexpr int NB = D * VF_BINS;
-  constexpr bool GAUSS = (INTEG == VF_INT_SYMGAUSS || INTEG == VF_INT_GAUSS);
-  float2* cells = reinterpret_cast<float2*>(smem);
-  float* hist = reinterpret_cast<float*>(smem + NB * sizeof(float2));
-  constexpr int NP = D / 2;  // joint pairs
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const int warp = tid >> 5;
-  const bool train = a.train != 0;
-  const bool limits = a.xmin != nullptr;
-  const int cpw = a.hist_copies;
-  const CallWords cw = call_words(a);
-  const bool fixedp = train && cpw == VF_F32_HIST_FIXED;
-  // fixed-point layout: integer joint tables (as layout 0), float overflow table [NB]
-  u32* hint = reinterpret_cast<u32*>(hist);
-  float* hovf = reinterpret_cast<float*>(hint + vegas_f32_joint_floats(D));
-
-  // ---- per-block float64 constants: Gaussian centres and k_d = sqrt(log2 e)/a_d,
-  // and the weight constant 50^D * xjac (* pref / prod k_d)
-  __shared__ double g_mu[D], g_k[D], g_wscale;
+// The float64 weight constant 50^D xjac (* pref / prod k for the Gaussian
+// family), times `sign`; thread 0 writes it, the caller syncs before reading it.
+template <int D, bool GAUSS, int INTEG>
+__device__ __forceinline__ void f32_block_constants(const SampleArgs& a, double* g_mu, double* g_k, double* g_wscale,
+                                                    double sign) {
   constexpr double SQRT_LOG2E = 1.2011224087864498;  // sqrt(log2(e))
+  const int tid = threadIdx.x;
   if (GAUSS && tid < D) {
     g_mu[tid] = (INTEG == VF_INT_SYMGAUSS) ? 0.5 : a.params[tid];
     g_k[tid] = SQRT_LOG2E / ((INTEG == VF_INT_SYMGAUSS) ? a.params[0] : a.params[D + tid]);
   }
   __syncthreads();
   if (tid == 0) {
-    double ws = a.xjac;
+    double ws = a.xjac * sign;
     for (int d = 0; d < D; ++d) ws *= 50.0;
     if (GAUSS) {
       double prodk = 1.0;
       for (int d = 0; d < D; ++d) prodk *= g_k[d];
       ws *= ((INTEG == VF_INT_SYMGAUSS) ? a.params[1] : 1.0) / prodk;
     }
-    g_wscale = ws;
+    *g_wscale = ws;
   }
+}
 
-  // ---- stage the per-bin table (float64, rounded once) and clear the histograms
-  for (int k = tid; k < NB; k += blockDim.x) {
+// The affine coefficients (c0, c1) of bin b of dimension d, in float64.
+template <bool GAUSS>
+__device__ __forceinline__ void f32_bin_affine(const SampleArgs& a, const double* g_mu, const double* g_k, int d,
+                                               int b, double& c0, double& c1) {
+  const double lo = a.grid[d * VF_EDGES + b];
+  const double dl = a.grid[d * VF_EDGES + b + 1] - lo;
+  c0 = lo - dl;
+  c1 = dl;
+  if (a.xmin != nullptr) {
+    c0 = a.xmin[d] + c0 * a.xdelta[d];
+    c1 = c1 * a.xdelta[d];
+  }
+  if (GAUSS) {
+    c0 = (c0 - g_mu[d]) * g_k[d];
+    c1 = c1 * g_k[d];
+  }
+}
+
+// ---- the Philox kernel -------------------------------------------------------
+
+// THREADS: the block size (1024 or 512; the launch-shape autotuner chooses),
+// with registers capped at 64 per thread (one 1024-thread or two 512-thread
+// blocks per SM).  TAP: the parity instantiation, which also writes every
+// event's D bin indices to a.ind_out ([n_events][D] int32); the kernels of the
+// hot path are TAP = false, where the writes do not exist.
+template <int D, int INTEG, int THREADS, bool TAP = false>
+__global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2048 / THREADS))
+vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NB = D * VF_BINS;
+  constexpr int NP = D / 2;
+  constexpr int PAIR = vegas_f32_pair_floats();
+  constexpr int DSTRIDE = VF_BINS * VF_F32_TC * 8;  // bytes per dimension of the table
+  constexpr bool GAUSS = (INTEG == VF_INT_SYMGAUSS || INTEG == VF_INT_GAUSS);
+  float2* cells = reinterpret_cast<float2*>(smem);
+  float* hist = reinterpret_cast<float*>(smem + vegas_f32_table_bytes(D));
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const bool train = a.train != 0;
+  const CallWords cw = call_words(a);
+
+  // ---- per-block float64 constants; the reversed, replicated table; histograms
+  __shared__ double g_mu[D], g_k[D], g_wscale;
+  f32_block_constants<D, GAUSS, INTEG>(a, g_mu, g_k, &g_wscale, (D & 1) ? -1.0 : 1.0);
+  for (int k = tid; k < NB; k += THREADS) {
     const int d = k / VF_BINS, b = k - d * VF_BINS;
-    const double lo = a.grid[d * VF_EDGES + b];
-    const double dl = a.grid[d * VF_EDGES + b + 1] - lo;
-    double c0 = lo - dl, c1 = dl;
-    if (limits) {
-      c0 = a.xmin[d] + c0 * a.xdelta[d];
-      c1 = c1 * a.xdelta[d];
-    }
-    if (GAUSS) {
-      c0 = (c0 - g_mu[d]) * g_k[d];
-      c1 = c1 * g_k[d];
-    }
-    cells[k] = make_float2((float)c0, (float)c1);
+    double c0, c1;
+    f32_bin_affine<GAUSS>(a, g_mu, g_k, d, b, c0, c1);
+    const float2 cell = make_float2((float)(c0 + 3.0 * c1), (float)(-c1));
+    float2* dst = cells + (d * VF_BINS + (VF_BINS - 1 - b)) * VF_F32_TC;
+#pragma unroll
+    for (int c = 0; c < VF_F32_TC; ++c) dst[c] = cell;
   }
-  if (train) {
-    if (cpw == 0)
-      for (int k = tid; k < NP * 2500 + (D & 1) * VF_BINS; k += blockDim.x) hist[k] = 0.0f;
-    else if (fixedp)
-      for (int k = tid; k < vegas_f32_joint_floats(D) + NB; k += blockDim.x) hint[k] = 0u;  // 0 and 0.0f
-    else
-      for (int k = tid; k < (THREADS / 32) * cpw * NB; k += blockDim.x) hist[k] = 0.0f;
-  }
+  if (train)
+    for (int k = tid; k < vegas_f32_hist_floats(D); k += THREADS) hist[k] = 0.0f;
   __syncthreads();
 
-  // float64 constant of the weight (host-computed): 50^D * xjac, times
-  // pref / prod k for the Gaussian family
-  const double wscale = g_wscale;
-  [[maybe_unused]] const float wscale_f = (float)wscale;  // the full weight handed to a user integrand
+  const double wscale = g_wscale;  // includes the weight's sign (-1)^D
+  [[maybe_unused]] const float wscale_f = (float)wscale;
   IntegrandConsts<float, D> kc;
   if (!GAUSS) load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
-
-  float* my_hist = hist + (warp * cpw + ((lane * cpw) >> 5)) * NB;
-  float hscale = 1.0f;  // fixed point: the block's power-of-two scale S
-  float qcap = 0.0f;    // fixed point: Qmax (0: the float table only)
+  // this lane's copy of the table
+  const char* mytab = reinterpret_cast<const char*>(cells + (lane & (VF_F32_TC - 1)));
   F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
 
-  // fixed point: add (w f)^2 of event `ev` to its D bins
-  auto add_fixed = [&](const int (&bins)[D], float v2, u64 ev) {
-    const float r = (float)((u32)ev * 0x9E3779B9u) * 2.3283064e-10f;  // Weyl dither in [0, 1)
-    const float q = fmaf(v2, hscale, r);
-    if (q < qcap) {
-      const u32 qi = __float2uint_rd(q);
-      if (qi != 0u) {
+  // one event's Philox words -> table cells j (reference bin 49 - j), weight,
+  // and the Gaussian exponent (or x)
+  auto draw = [&](u64 ev, int (&bins)[D], float& wf, float& s, float (&x)[D]) {
 #pragma unroll
-        for (int p = 0; p < NP; ++p)
-          atomicAdd(hint + p * 2500 + (bins[2 * p] - 2 * p * VF_BINS) * VF_BINS +
-                        (bins[2 * p + 1] - (2 * p + 1) * VF_BINS),
-                    qi);
-        if (D & 1) atomicAdd(hint + NP * 2500 + (bins[D - 1] - (D - 1) * VF_BINS), qi);
+    for (int q = 0; q < (D + 3) / 4; ++q) {
+      u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = cw.c2base | (u32)q, c3 = cw.c3;
+      philox4x32_10_rk(c0, c1, c2, c3, a.rk);
+      const u32 wq[4] = {c0, c1, c2, c3};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int d = 4 * q + j;
+        if (d < D) {
+          const u64 pp = (u64)wq[j] * 50ull + 25ull;
+          const u32 jj = (u32)(pp >> 32);
+          const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
+          const float2 c = *reinterpret_cast<const float2*>(mytab + (jj << 7) + d * DSTRIDE);
+          const float t = fmaf(c.y, m, c.x);
+          wf = (d == 0) ? c.y : wf * c.y;
+          if (GAUSS)
+            s = fmaf(t, t, s);
+          else
+            x[d] = t;
+          bins[d] = (int)jj;
+        }
       }
-    } else {
-#pragma unroll
-      for (int d = 0; d < D; ++d) atomicAdd(hovf + bins[d], v2);
     }
   };
 
-  // one event from its per-dimension (bin, m) pairs; returns (w f)^2
-  auto finish = [&](const int (&bins)[D], float wf, float s, const float (&x)[D]) -> float {
+  // one event from its cells: the integrand, the sums and the histogram
+  auto finish = [&](const int (&bins)[D], float wf, float s, const float (&x)[D]) {
     float f;
     if constexpr (GAUSS) {
       f = ex2_approx_ftz(-s);
@@ -253,241 +287,48 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
     const float v2 = v * v;
     two_sum_add(s1, v);
     two_sum_add(s2, v2);
-    if (train && !fixedp) {
-      if (cpw == 0) {
+    if (train) {
 #pragma unroll
-        for (int p = 0; p < NP; ++p)
-          atomicAdd(hist + p * 2500 + (bins[2 * p] - 2 * p * VF_BINS) * VF_BINS +
-                        (bins[2 * p + 1] - (2 * p + 1) * VF_BINS),
-                    v2);
-        if (D & 1) atomicAdd(hist + NP * 2500 + (bins[D - 1] - (D - 1) * VF_BINS), v2);
-      } else {
-#pragma unroll
-        for (int d = 0; d < D; ++d) atomicAdd(my_hist + bins[d], v2);
-      }
+      for (int p = 0; p < NP; ++p) atomicAdd(hist + p * PAIR + joint_cell(bins[2 * p], bins[2 * p + 1]), v2);
+      if (D & 1) atomicAdd(hist + NP * PAIR + bins[D - 1], v2);
     }
-    return v2;
   };
 
-  // parity tap: the event's bin indices (bins[] holds d 50 + bin)
-  auto tap = [&](long long ev_idx, const int (&bins)[D]) {
+  // parity tap: the reference's bin indices of the event
+  auto tap = [&](long long e, const int (&bins)[D]) {
     if constexpr (TAP) {
 #pragma unroll
-      for (int d = 0; d < D; ++d) a.ind_out[ev_idx * D + d] = bins[d] - d * VF_BINS;
-    }
-  };
-
-  // one event's Philox words -> bins, weight and the Gaussian exponent (or x)
-  auto draw = [&](u64 ev, int (&bins)[D], float& wf, float& s, float (&x)[D]) {
-#pragma unroll
-    for (int q = 0; q < (D + 3) / 4; ++q) {
-      u32 c0 = (u32)ev, c1 = (u32)(ev >> 32), c2 = cw.c2base | (u32)q, c3 = cw.c3;
-      philox4x32_10_rk(c0, c1, c2, c3, a.rk);
-      const u32 wq[4] = {c0, c1, c2, c3};
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int d = 4 * q + j;
-        if (d < D) {
-          const u64 pp = (u64)(~wq[j]) * 50ull + 25ull;
-          const int i = (int)(pp >> 32);
-          const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
-          const float2 c = cells[d * VF_BINS + i];
-          const float t = fmaf(c.y, m, c.x);
-          wf = (d == 0) ? c.y : wf * c.y;
-          if (GAUSS)
-            s = fmaf(t, t, s);
-          else
-            x[d] = t;
-          bins[d] = d * VF_BINS + i;
-        }
-      }
+      for (int d = 0; d < D; ++d) a.ind_out[e * D + d] = VF_BINS - 1 - bins[d];
     }
   };
 
   const long long n = a.n_events;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  long long e = (long long)blockIdx.x * blockDim.x + tid;
-  if (a.u_inj == nullptr) {
-    if (fixedp) {
-      // Qmax from the most events the block walks, and the block's scale from
-      // the first event of every thread: S = 2^k, k = floor(log2 Qmax) - 9 -
-      // round(mean log2 (w f)^2) over the normal finite values
-      __shared__ float lsum[THREADS / 32];
-      __shared__ int lcnt[THREADS / 32];
-      int bins[D];
-      float x[D];
-      float wf = 1.0f, s = 0.0f, v2 = 0.0f;
-      const u64 ev = (u64)(a.ev_offset + e);
-      const bool have = e < n;
-      if (have) {
-        draw(ev, bins, wf, s, x);
-        v2 = finish(bins, wf, s, x);
-        tap(e, bins);
-      }
-      const bool use = have && v2 >= 1.17549435e-38f && v2 <= 3.40282347e38f;  // normal, finite
-      float l = use ? __log2f(v2) : 0.0f;
-      int c = use ? 1 : 0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        l += __shfl_xor_sync(0xffffffffu, l, o);
-        c += __shfl_xor_sync(0xffffffffu, c, o);
-      }
-      if (lane == 0) {
-        lsum[warp] = l;
-        lcnt[warp] = c;
-      }
-      __syncthreads();
-      float ls = 0.0f;
-      int cs = 0;
-#pragma unroll
-      for (int i = 0; i < THREADS / 32; ++i) {
-        ls += lsum[i];
-        cs += lcnt[i];
-      }
-      const long long per_thread = n > 0 ? (n + stride - 1) / stride : 1;
-      const float cap = floorf((float)(4294967295.0 / ((double)THREADS * (double)per_thread)));
-      const int cap_log2 = (int)((__float_as_uint(cap) >> 23) & 0xFF) - 127;  // floor(log2 Qmax)
-      int k = cap_log2 - 9 - (cs > 0 ? __float2int_rn(ls / (float)cs) : 0);
-      k = k < -126 ? -126 : (k > 127 ? 127 : k);
-      hscale = __int_as_float((127 + k) << 23);  // 2^k
-      qcap = cs > 0 ? cap : 0.0f;
-      if (have) add_fixed(bins, v2, ev);
-      e += stride;
+  const long long stride = (long long)gridDim.x * THREADS;
+  long long e = (long long)blockIdx.x * THREADS + tid;
+  // Two events per pass give the scheduler two independent draws to overlap
+  // (shared-memory latency of one with the Philox rounds of the other); the
+  // registers it needs pay for themselves only at small D.
+  if constexpr (D <= 4) {
+    for (; e + stride < n; e += 2 * stride) {
+      const u64 ev0 = (u64)(a.ev_offset + e), ev1 = ev0 + (u64)stride;
+      int b0[D], b1[D];
+      float x0[D], x1[D];
+      float wf0 = 1.0f, s0 = 0.0f, wf1 = 1.0f, s1_ = 0.0f;
+      draw(ev0, b0, wf0, s0, x0);
+      draw(ev1, b1, wf1, s1_, x1);
+      finish(b0, wf0, s0, x0);
+      finish(b1, wf1, s1_, x1);
+      tap(e, b0);
+      tap(e + stride, b1);
     }
-    // Two events per pass give the scheduler two independent draws to overlap
-    // (shared-memory latency of one with the Philox rounds of the other).
-    // Measured (1e8 events): faster for D <= 4 (0.560 vs 0.582 ms training,
-    // 0.441 vs 0.490 frozen).  For D >= 5 it made frozen grids faster too (D = 8:
-    // 0.717 vs 0.799 ms) but training slower (D = 8: 0.984 vs 0.975 ms, the
-    // histogram atomics dominate), and the registers it needs slow the training
-    // loop even where it is not taken, so it is compiled for D <= 4 only.
-    if constexpr (D <= 4) if (!fixedp) {
-      for (; e + stride < n; e += 2 * stride) {
-        const u64 ev0 = (u64)(a.ev_offset + e), ev1 = ev0 + (u64)stride;
-        int b0[D], b1[D];
-        float x0[D], x1[D];
-        float wf0 = 1.0f, s0 = 0.0f, wf1 = 1.0f, s1_ = 0.0f;
-        draw(ev0, b0, wf0, s0, x0);
-        draw(ev1, b1, wf1, s1_, x1);
-        finish(b0, wf0, s0, x0);
-        finish(b1, wf1, s1_, x1);
-        tap(e, b0);
-        tap(e + stride, b1);
-      }
-    }
-    for (; e < n; e += stride) {
-      const u64 ev = (u64)(a.ev_offset + e);
-      int bins[D];
-      float x[D];
-      float wf = 1.0f, s = 0.0f;
-      draw(ev, bins, wf, s, x);
-      const float v2 = finish(bins, wf, s, x);
-      if (fixedp) add_fixed(bins, v2, ev);
-      tap(e, bins);
-    }
-  } else {
-    // injected float64 uniforms, [n][D] row-major, streamed once
-    int bad = 0;
-    auto injected_event = [&](const u64 (&ub)[D], long long ev_idx) {
-      int bins[D];
-      float x[D];
-      float wf = 1.0f, s = 0.0f;
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        int i;
-        float m;
-        if (!inj_bin_exact(ub[d], i, m)) {
-          // the bin in float64, bit-exact with the reference (vflow.py:117, :67)
-          const double xn = __dmul_rn(50.0, __dsub_rn(1.0, __longlong_as_double((long long)ub[d])));
-          i = (int)xn;
-          if (i < 0 || i > VF_BINS - 1) {
-            bad = 1;
-            i = i < 0 ? 0 : VF_BINS - 1;
-          }
-          m = (float)(1.0 + (xn - floor(xn)));
-        }
-        const float2 c = cells[d * VF_BINS + i];
-        const float t = fmaf(c.y, m, c.x);
-        wf = (d == 0) ? c.y : wf * c.y;
-        if (GAUSS)
-          s = fmaf(t, t, s);
-        else
-          x[d] = t;
-        bins[d] = d * VF_BINS + i;
-      }
-      const float v2 = finish(bins, wf, s, x);
-      if (fixedp)  // injected uniforms: the float table, no scale
-        for (int d = 0; d < D; ++d) atomicAdd(hovf + bins[d], v2);
-      tap(ev_idx, bins);
-    };
-    if (a.tma_swizzle != 0 && (D == 4 || D == 8 || D == 16)) {
-      // Tiles of THREADS events (the grid-stride assignment: tile t holds
-      // events t THREADS .. t THREADS + THREADS - 1, thread i takes event i)
-      // brought in by TMA into one shared-memory stage; the tensor map's
-      // swizzle (32/64/128 bytes for rows of 32/64/128 bytes) makes every
-      // quarter-warp read of a row conflict-free.  Each thread copies its row to
-      // registers, the block syncs, the next tile's copy is issued and then the
-      // events are evaluated, so the copy overlaps the arithmetic with a
-      // single 8 D THREADS-byte stage (registers are the second buffer).
-      constexpr int ROWB = 8 * D;
-      constexpr u32 TILEB = THREADS * ROWB;  // a multiple of 1024
-      __shared__ alignas(8) u64 tma_bar;
-      const u32 stage =
-          (smem_u32(smem) + (u32)vegas_f32_smem_bytes(D, cpw, a.train, THREADS) + 1023u) & ~1023u;
-      const u32 bar = smem_u32(&tma_bar);
-      const long long n_tiles = (n + THREADS - 1) / THREADS;
-      const long long G = gridDim.x;
-      if (tid == 0) {
-        mbar_init(bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        if (blockIdx.x < n_tiles) tma_load_tile(stage, a.tmap, 0, (int)(blockIdx.x * THREADS), bar, TILEB);
-      }
-      __syncthreads();
-      const u32 swz = (1u << a.tma_swizzle) - 1u;
-      u32 parity = 0;
-      for (long long t = blockIdx.x; t < n_tiles; t += G) {
-        const bool ok = mbar_wait_bounded(bar, parity);
-        parity ^= 1u;
-        if (!__syncthreads_and(ok)) {  // a copy never completed: report, stop
-          if (tid == 0 && a.flags) atomicOr(a.flags, VF_FLAG_TIMEOUT);
-          break;
-        }
-        u64 ub[D];
-#pragma unroll
-        for (int j = 0; j < D / 2; ++j) {
-          const u32 off = (u32)(tid * ROWB + 16 * j);
-          const u32 addr = stage + (off ^ (((off >> 7) & swz) << 4));
-          asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(ub[2 * j]), "=l"(ub[2 * j + 1]) : "r"(addr));
-        }
-        __syncthreads();  // the stage is read: refill it while the events are evaluated
-        if (tid == 0 && t + G < n_tiles) {
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          tma_load_tile(stage, a.tmap, 0, (int)((t + G) * THREADS), bar, TILEB);
-        }
-        if (t * THREADS + tid < n) injected_event(ub, t * THREADS + tid);
-      }
-    } else {
-      // plain loads: 16-byte (evict-first) when D is even and the array is
-      // 16-byte aligned
-      const bool vec = (D % 2 == 0) && ((reinterpret_cast<size_t>(a.u_inj) & 15) == 0);
-      for (; e < n; e += stride) {
-        const long long* up = reinterpret_cast<const long long*>(a.u_inj) + e * D;
-        u64 ub[D];
-        if (vec) {
-#pragma unroll
-          for (int j = 0; j < D / 2; ++j) {
-            const longlong2 v = __ldcs(reinterpret_cast<const longlong2*>(up) + j);
-            ub[2 * j] = (u64)v.x;
-            ub[2 * j + 1] = (u64)v.y;
-          }
-        } else {
-#pragma unroll
-          for (int d = 0; d < D; ++d) ub[d] = (u64)__ldcs(up + d);
-        }
-        injected_event(ub, e);
-      }
-    }
-    if (bad && a.flags) atomicOr(a.flags, VF_FLAG_INDEX_RANGE);
+  }
+  for (; e < n; e += stride) {
+    int bins[D];
+    float x[D];
+    float wf = 1.0f, s = 0.0f;
+    draw((u64)(a.ev_offset + e), bins, wf, s, x);
+    finish(bins, wf, s, x);
+    tap(e, bins);
   }
 
   // ---- block partials: TwoSum merges across the warp and the block, float64 row
@@ -519,43 +360,21 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
     }
   }
   if (train) {
-    // marginals / copy sums in fp32 (the tables are fp32), one float64 scaling per bin
+    // marginals in fp32 (the tables are fp32), one float64 scaling per bin;
+    // bin b of a dimension is its table's cell 49 - b
     const double s2c = wscale * wscale;
-    const int ncopies = (THREADS / 32) * cpw;
-    for (int k = tid; k < NB; k += blockDim.x) {
+    for (int k = tid; k < NB; k += THREADS) {
+      const int d = k / VF_BINS, b = k - d * VF_BINS;
+      const int jb = VF_BINS - 1 - b;
       float hf = 0.0f;
-      if (cpw == 0) {
-        const int d = k / VF_BINS, b = k - d * VF_BINS;
-        if (d < 2 * NP) {
-          const float* tab = hist + (d >> 1) * 2500;
-          if ((d & 1) == 0)
-            for (int c = 0; c < VF_BINS; ++c) hf += tab[b * VF_BINS + c];  // row sum
-          else
-            for (int r = 0; r < VF_BINS; ++r) hf += tab[r * VF_BINS + b];  // column sum
-        } else {
-          hf = hist[NP * 2500 + b];
-        }
-      } else if (fixedp) {
-        const int d = k / VF_BINS, b = k - d * VF_BINS;
-        u64 total = 0;
-        if (d < 2 * NP) {
-          const u32* tab = hint + (d >> 1) * 2500;
-          if ((d & 1) == 0)
-            for (int c = 0; c < VF_BINS; ++c) total += tab[b * VF_BINS + c];  // row sum
-          else
-            for (int r = 0; r < VF_BINS; ++r) total += tab[r * VF_BINS + b];  // column sum
-        } else {
-          total = hint[NP * 2500 + b];
-        }
-        hf = hovf[k];
-        const double h = ((double)total / (double)hscale + (double)hf) * s2c;
-        if (a.accumulate)
-          row[2 + k] += h;
+      if (d < 2 * NP) {
+        const float* tab = hist + (d >> 1) * PAIR;
+        if ((d & 1) == 0)
+          for (int c = 0; c < VF_F32_JOINT_ROW; ++c) hf += tab[jb * VF_F32_JOINT_ROW + c];  // row sum
         else
-          row[2 + k] = h;
-        continue;
+          for (int r = 0; r < VF_BINS; ++r) hf += tab[joint_cell(r, jb)];  // column sum
       } else {
-        for (int c = 0; c < ncopies; ++c) hf += hist[c * NB + k];
+        hf = hist[NP * PAIR + jb];
       }
       const double h = (double)hf * s2c;
       if (a.accumulate)
@@ -567,7 +386,295 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
   // rows beyond the grid (a launch with fewer blocks than the caller's rows)
   if (!a.accumulate)
     for (long long r = blockIdx.x + (long long)gridDim.x; r < a.rows_total; r += gridDim.x)
-      for (int k = tid; k < W; k += blockDim.x) a.partials[r * W + k] = 0.0;
+      for (int k = tid; k < W; k += THREADS) a.partials[r * W + k] = 0.0;
+}
+
+// ---- the injected-uniform kernel ----------------------------------------------
+//
+// Injected float64 uniforms ([n][D] row-major, streamed once) with the
+// reference's float64 bin of every uniform (inj_bin_exact, or the float64
+// operations in its rare cases).  1024 threads per block (one block per SM) in
+// VF_INJ_GROUPS groups of VF_INJ_ROWS threads.  With a.tma_swizzle set (D = 4,
+// 8, 16 and a 16-byte aligned array) each group streams its own tiles of
+// VF_INJ_ROWS events (thread r of the group takes row r) through a ring of
+// `stages` shared-memory stages filled by TMA tensor copies (the tensor map's
+// 32/64/128-byte swizzle makes every quarter-warp read of a row
+// conflict-free): a thread copies its row to registers, the group meets at its
+// named barrier, its first thread issues the copy of the tile `stages` ahead
+// into the freed stage, and the events are evaluated while the copies land --
+// four groups keep up to 4 `stages` tiles in flight per SM.  Otherwise plain
+// loads (16-byte, evict-first when D is even and the array is aligned).
+// The bin table is lane-replicated as in the Philox kernel but in bin order,
+// the histogram joint pair tables have 50-float rows.
+
+#define VF_INJ_THREADS 1024
+#define VF_INJ_ROWS 256
+#define VF_INJ_GROUPS (VF_INJ_THREADS / VF_INJ_ROWS)
+#define VF_SMEM_LIMIT 232448  // dynamic shared memory a block may use (227 KB)
+
+// Table copies and stages per group of the injected kernel for dimension D
+// (the largest that fit in shared memory; stages = 0: no TMA path for this D).
+// With the TMA ring, 1024 bytes of slack in front of it let the ring start on
+// a 1024-byte boundary wherever the dynamic shared memory begins.
+__host__ __device__ constexpr int inj_tma_dim(int D) { return D == 4 || D == 8 || D == 16; }
+__host__ __device__ constexpr int inj_table_bytes(int D, int tc) { return D * VF_BINS * tc * 8; }
+__host__ __device__ constexpr int inj_hist_bytes(int D) { return ((D / 2) * 2500 + (D & 1) * VF_BINS) * 4; }
+__host__ __device__ constexpr int inj_tile_bytes(int D) { return VF_INJ_ROWS * 8 * D; }
+__host__ __device__ constexpr int inj_fit(int D, int tc, int st) {
+  return inj_table_bytes(D, tc) + inj_hist_bytes(D) + (st ? 1024 : 0) + VF_INJ_GROUPS * st * inj_tile_bytes(D) <=
+         VF_SMEM_LIMIT;
+}
+__host__ __device__ constexpr int inj_tc(int D) {
+  return !inj_tma_dim(D) ? (inj_fit(D, 16, 0) ? 16 : 1)
+                         : (inj_fit(D, 16, 2) ? 16 : (inj_fit(D, 1, 2) ? 1 : (inj_fit(D, 16, 1) ? 16 : 1)));
+}
+__host__ __device__ constexpr int inj_stages(int D) {
+  return !inj_tma_dim(D) ? 0 : (inj_fit(D, inj_tc(D), 2) ? 2 : 1);
+}
+// Dynamic shared memory of the injected kernel: table and histogram, and with
+// `tma` the stage ring (with its 1024 bytes of slack).
+__host__ __device__ inline int vegas_f32_inj_smem_bytes(int D, int train, bool tma = false) {
+  const int base = inj_table_bytes(D, inj_tc(D)) + (train ? inj_hist_bytes(D) : 0);
+  if (!tma || !inj_tma_dim(D)) return base;
+  return base + 1024 + VF_INJ_GROUPS * inj_stages(D) * inj_tile_bytes(D);
+}
+
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// All threads of named barrier `id` (count threads) vote: whether every one has `ok`.
+__device__ __forceinline__ bool named_all(int id, int count, bool ok) {
+  u32 r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(r)
+      : "r"((u32)ok), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
+
+template <int D, int INTEG, bool TAP = false>
+__global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(const __grid_constant__ SampleArgs a) {
+  constexpr int THREADS = VF_INJ_THREADS;
+  constexpr int TC = inj_tc(D);
+  constexpr int STAGES = inj_stages(D);
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NB = D * VF_BINS;
+  constexpr int NP = D / 2;
+  constexpr int DSTRIDE = VF_BINS * TC * 8;
+  constexpr bool GAUSS = (INTEG == VF_INT_SYMGAUSS || INTEG == VF_INT_GAUSS);
+  float2* cells = reinterpret_cast<float2*>(smem);
+  float* hist = reinterpret_cast<float*>(smem + inj_table_bytes(D, TC));
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const bool train = a.train != 0;
+
+  // the TMA path's barriers: one per stage of every group, initialised before
+  // the block-wide sync below
+  __shared__ alignas(8) u64 tma_bar[VF_INJ_GROUPS][STAGES > 0 ? STAGES : 1];
+  const bool tma = STAGES > 0 && a.tma_swizzle != 0;
+  if (tma && tid == 0) {
+    for (int gg = 0; gg < VF_INJ_GROUPS; ++gg)
+      for (int st = 0; st < STAGES; ++st) mbar_init(smem_u32(&tma_bar[gg][st]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __shared__ double g_mu[D], g_k[D], g_wscale;
+  f32_block_constants<D, GAUSS, INTEG>(a, g_mu, g_k, &g_wscale, 1.0);
+  for (int k = tid; k < NB; k += THREADS) {
+    const int d = k / VF_BINS, b = k - d * VF_BINS;
+    double c0, c1;
+    f32_bin_affine<GAUSS>(a, g_mu, g_k, d, b, c0, c1);
+    const float2 cell = make_float2((float)c0, (float)c1);
+#pragma unroll
+    for (int c = 0; c < TC; ++c) cells[k * TC + c] = cell;
+  }
+  if (train)
+    for (int k = tid; k < inj_hist_bytes(D) / 4; k += THREADS) hist[k] = 0.0f;
+  __syncthreads();  // constants, table, histogram and barriers ready
+
+  const double wscale = g_wscale;
+  [[maybe_unused]] const float wscale_f = (float)wscale;
+  IntegrandConsts<float, D> kc;
+  if (!GAUSS) load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
+  const char* mytab = reinterpret_cast<const char*>(cells + (lane & (TC - 1)));
+  F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
+  int bad = 0;
+
+  auto event = [&](const u64 (&ub)[D], long long e) {
+    int bins[D];
+    float x[D];
+    float wf = 1.0f, s = 0.0f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      int i;
+      float m;
+      if (!inj_bin_exact(ub[d], i, m)) {
+        // the bin in float64, bit-exact with the reference (vflow.py:117, :67)
+        const double xn = __dmul_rn(50.0, __dsub_rn(1.0, __longlong_as_double((long long)ub[d])));
+        i = (int)xn;
+        if (i < 0 || i > VF_BINS - 1) {
+          bad = 1;
+          i = i < 0 ? 0 : VF_BINS - 1;
+        }
+        m = (float)(1.0 + (xn - floor(xn)));
+      }
+      const float2 c = *reinterpret_cast<const float2*>(mytab + i * (TC * 8) + d * DSTRIDE);
+      const float t = fmaf(c.y, m, c.x);
+      wf = (d == 0) ? c.y : wf * c.y;
+      if (GAUSS)
+        s = fmaf(t, t, s);
+      else
+        x[d] = t;
+      bins[d] = i;
+    }
+    float f;
+    if constexpr (GAUSS) {
+      f = ex2_approx_ftz(-s);
+    } else {
+#ifdef VF_JIT_USER
+      if constexpr (INTEG == VF_INT_USER)
+        f = (float)VF_USER_FN(x, D, wf * wscale_f, a.params);
+      else
+#endif
+        f = eval_builtin<D>(INTEG, x, D, kc);
+    }
+    const float v = wf * f;
+    const float v2 = v * v;
+    two_sum_add(s1, v);
+    two_sum_add(s2, v2);
+    if (train) {
+#pragma unroll
+      for (int p = 0; p < NP; ++p) atomicAdd(hist + p * 2500 + bins[2 * p] * VF_BINS + bins[2 * p + 1], v2);
+      if (D & 1) atomicAdd(hist + NP * 2500 + bins[D - 1], v2);
+    }
+    if constexpr (TAP) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) a.ind_out[e * D + d] = bins[d];
+    }
+  };
+
+  const long long n = a.n_events;
+  if constexpr (STAGES > 0) {
+    if (tma) {
+      constexpr int ROWB = 8 * D;
+      constexpr u32 TILEB = inj_tile_bytes(D);  // a multiple of 1024
+      const u32 ring = (smem_u32(smem) + (u32)vegas_f32_inj_smem_bytes(D, a.train) + 1023u) & ~1023u;
+      const int g = tid / VF_INJ_ROWS, r = tid % VF_INJ_ROWS;
+      const u32 stage0 = ring + (u32)(g * STAGES) * TILEB;
+      const long long n_tiles = (n + VF_INJ_ROWS - 1) / VF_INJ_ROWS;
+      // the group's tiles: first, first + step, ...
+      const long long step = (long long)gridDim.x * VF_INJ_GROUPS;
+      const long long first = (long long)blockIdx.x * VF_INJ_GROUPS + g;
+      if (r == 0)
+        for (int st = 0; st < STAGES; ++st) {
+          const long long t = first + st * step;
+          if (t < n_tiles)
+            tma_load_tile(stage0 + (u32)st * TILEB, a.tmap, 0, (int)(t * VF_INJ_ROWS), smem_u32(&tma_bar[g][st]),
+                          TILEB);
+        }
+      const u32 swz = (1u << a.tma_swizzle) - 1u;
+      int k = 0;
+      for (long long t = first; t < n_tiles; t += step, ++k) {
+        const int st = k % STAGES;
+        const u32 stage = stage0 + (u32)st * TILEB;
+        const bool ok = mbar_wait_bounded(smem_u32(&tma_bar[g][st]), (u32)((k / STAGES) & 1));
+        if (!named_all(1 + g, VF_INJ_ROWS, ok)) {  // a copy never completed: report, stop this group
+          if (r == 0 && a.flags) atomicOr(a.flags, VF_FLAG_TIMEOUT);
+          break;
+        }
+        u64 ub[D];
+#pragma unroll
+        for (int j = 0; j < D / 2; ++j) {
+          const u32 off = (u32)(r * ROWB + 16 * j);
+          const u32 addr = stage + (off ^ (((off >> 7) & swz) << 4));
+          asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(ub[2 * j]), "=l"(ub[2 * j + 1]) : "r"(addr));
+        }
+        named_sync(1 + g, VF_INJ_ROWS);  // the stage is read: refill it while the events are evaluated
+        if (r == 0 && t + STAGES * step < n_tiles) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          tma_load_tile(stage, a.tmap, 0, (int)((t + STAGES * step) * VF_INJ_ROWS), smem_u32(&tma_bar[g][st]),
+                        TILEB);
+        }
+        const long long e = t * VF_INJ_ROWS + r;
+        if (e < n) event(ub, e);
+      }
+    }
+  }
+  if (!tma) {
+    const long long stride = (long long)gridDim.x * THREADS;
+    const bool vec = (D % 2 == 0) && ((reinterpret_cast<size_t>(a.u_inj) & 15) == 0);
+    for (long long e = (long long)blockIdx.x * THREADS + tid; e < n; e += stride) {
+      const long long* up = reinterpret_cast<const long long*>(a.u_inj) + e * D;
+      u64 ub[D];
+      if (vec) {
+#pragma unroll
+        for (int j = 0; j < D / 2; ++j) {
+          const longlong2 v = __ldcs(reinterpret_cast<const longlong2*>(up) + j);
+          ub[2 * j] = (u64)v.x;
+          ub[2 * j + 1] = (u64)v.y;
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < D; ++d) ub[d] = (u64)__ldcs(up + d);
+      }
+      event(ub, e);
+    }
+  }
+  if (bad && a.flags) atomicOr(a.flags, VF_FLAG_INDEX_RANGE);
+
+  __shared__ double red[2][THREADS / 32];
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  if (lane == 0) {
+    red[0][warp] = (double)s1.s + (double)s1.c;
+    red[1][warp] = (double)s2.s + (double)s2.c;
+  }
+  __syncthreads();
+  const int W = 2 + NB;
+  double* row = a.partials + (long long)blockIdx.x * W;
+  if (tid == 0) {
+    double b1 = 0.0, b2 = 0.0;
+    for (int i = 0; i < THREADS / 32; ++i) {
+      b1 += red[0][i];
+      b2 += red[1][i];
+    }
+    b1 *= wscale;
+    b2 *= wscale * wscale;
+    if ((!isfinite(b1) || !isfinite(b2)) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
+    if (a.accumulate) {
+      row[0] += b1;
+      row[1] += b2;
+    } else {
+      row[0] = b1;
+      row[1] = b2;
+    }
+  }
+  if (train) {
+    const double s2c = wscale * wscale;
+    for (int k = tid; k < NB; k += THREADS) {
+      const int d = k / VF_BINS, b = k - d * VF_BINS;
+      float hf = 0.0f;
+      if (d < 2 * NP) {
+        const float* tab = hist + (d >> 1) * 2500;
+        if ((d & 1) == 0)
+          for (int c = 0; c < VF_BINS; ++c) hf += tab[b * VF_BINS + c];  // row sum
+        else
+          for (int rr = 0; rr < VF_BINS; ++rr) hf += tab[rr * VF_BINS + b];  // column sum
+      } else {
+        hf = hist[NP * 2500 + b];
+      }
+      const double h = (double)hf * s2c;
+      if (a.accumulate)
+        row[2 + k] += h;
+      else
+        row[2 + k] = h;
+    }
+  }
+  if (!a.accumulate)
+    for (long long rr = blockIdx.x + (long long)gridDim.x; rr < a.rows_total; rr += gridDim.x)
+      for (int k = tid; k < W; k += THREADS) a.partials[rr * W + k] = 0.0;
 }
 
 }  // namespace vf

@@ -1,5 +1,5 @@
-// Parity instantiations of the fp32 VEGAS sampler (TAP = true: every event's
-// bin indices written to ind_out), 256 threads per block, dimensions 1-16, for
+// Parity instantiations of the fp32 VEGAS Philox sampler (TAP = true: every
+// event's bin indices written to ind_out), 1024 threads per block, dimensions 1-16, for
 // the symmetric Gaussian (the benchmarked integrand) and the product integrand
 // (whose table holds the point itself).  Tests reach them through vf_sample
 // with ind_out as the only tap.
@@ -11,8 +11,8 @@ namespace vf {
 template <int D>
 static const void* pick_tap(int integrand) {
   switch (integrand) {
-    case VF_INT_SYMGAUSS: return (const void*)vf_vegas_f32_kernel<D, VF_INT_SYMGAUSS, 256, true>;
-    case VF_INT_PROD: return (const void*)vf_vegas_f32_kernel<D, VF_INT_PROD, 256, true>;
+    case VF_INT_SYMGAUSS: return (const void*)vf_vegas_f32_kernel<D, VF_INT_SYMGAUSS, 1024, true>;
+    case VF_INT_PROD: return (const void*)vf_vegas_f32_kernel<D, VF_INT_PROD, 1024, true>;
     default: return nullptr;
   }
 }
