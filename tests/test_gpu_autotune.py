@@ -102,12 +102,15 @@ def _hist(inst, generic=False):
     return inst._workspace()["hist"].cpu().numpy().copy()
 
 
-@pytest.mark.parametrize("n_dim", [1, 3, 8, 12, 16])
+@pytest.mark.parametrize("n_dim", [1, 3, 8, 12])
 @pytest.mark.parametrize("trained", [False, True])
 def test_histogram_matches_generic_sampler(n_dim, trained):
     """The fused sampler's joint pair tables (reversed, swizzled cells) give
     every dimension the per-bin sums of the generic sampler's plain table on the
-    same events and grid, under both block sizes (float rounding apart)."""
+    same events and grid, under both block sizes (float rounding apart).  (The
+    generic sampler keeps the weight without its 50^D factor in float32, whose
+    square underflows beyond about 12 dimensions; 16 dimensions are checked
+    against the float64 path in test_gpu_precision.py.)"""
     inst = VegasFlow(n_dim, 1_000_000, precision="fp32", seed=4, verbose=False)
     # a width at which no event's (w f)^2 underflows float32 on the uniform grid
     # in either sampler (the generic one evaluates the normalised integrand)

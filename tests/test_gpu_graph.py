@@ -37,8 +37,17 @@ def _pair(cls, precision, integrand, n_dim=4, n=100_000, **kw):
     return out
 
 
+# fp32: graph replays and eager launches run the same kernels on the same
+# events, but the histogram's float atomics commit in whatever order the warps
+# reach them, so the float32 refinement's grids (and the later iterations'
+# results) agree to float32 rounding of the histogram, not bit for bit: the
+# grid tolerance is the fp32 refinement's own (it agrees with the float64
+# refinement to 2e-5).
+FP32_GRID_ATOL = 2e-5
+
+
 def _rtol(precision):
-    return 1e-10 if precision == "fp64" else 2e-6
+    return 1e-10 if precision == "fp64" else 1e-5
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
@@ -49,7 +58,7 @@ def test_vegas_graph_matches_eager(precision):
         r_g = graph.run_integration(5)
         np.testing.assert_allclose(r_g, r_e, rtol=_rtol(precision))
     np.testing.assert_allclose(graph.divisions.cpu().numpy(), eager.divisions.cpu().numpy(), rtol=0,
-                               atol=1e-12 if precision == "fp64" else 1e-6)
+                               atol=1e-12 if precision == "fp64" else FP32_GRID_ATOL)
     assert graph._call_ctr == eager._call_ctr == 10
     hist_e = [h[:2] for h in eager._history]
     hist_g = [h[:2] for h in graph._history]
@@ -105,7 +114,7 @@ def test_plus_graph_matches_eager(precision, adaptive):
     if adaptive:
         assert graph.n_events != n0  # reallocated on the device
     np.testing.assert_allclose(graph.divisions.cpu().numpy(), eager.divisions.cpu().numpy(), rtol=0,
-                               atol=1e-12 if precision == "fp64" else 1e-6)
+                               atol=1e-12 if precision == "fp64" else FP32_GRID_ATOL)
     graph.run_integration(2)
     assert graph._graph is g1  # reading n_events does not force a new capture
     assert abs(r_g[0] - math.erf(2.5) ** 3) < 5 * r_g[1]

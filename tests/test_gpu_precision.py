@@ -22,6 +22,7 @@ import torch
 
 import oracle
 from vegasflow_gb300 import VegasFlow, VegasFlowPlus, integrands
+from vegasflow_gb300 import _native as nat
 from vegasflow_gb300.batch import VegasBatch, c4_specs
 
 pytestmark = pytest.mark.gpu
@@ -117,4 +118,31 @@ def test_c4_batch_fp32_against_oracle_on_its_own_events():
         r64, s64 = orc.iteration(rows, lambda x: oracle.integrand_gauss_mu(x, p[:d], p[d:]))
         pulls.append((hist[k, 0] - r64) / s64)
     print(f"C4 batched fp32 - fp64 (sigma units) over {len(picks)} integrals: {np.round(pulls, 4)}")
+    assert np.all(np.abs(pulls) < BAR), pulls
+
+
+@pytest.mark.parametrize("which", ["prod", "symgauss"])
+def test_high_dimension_fp32_against_float64_on_its_own_events(which):
+    """16 dimensions, where an event's weight prod_d delta is ~50^-16: the fused
+    fp32 sampler (its weight prescaled by a power of two) against the float64
+    path on the same events (vf_philox_uniforms) and grid, every iteration of a
+    trained run -- result and sigma."""
+    n_dim, n, seed = 16, 2_000_000, 19
+    f = integrands.prod() if which == "prod" else integrands.symgauss(0.3)
+    f32 = VegasFlow(n_dim, n, verbose=False, precision="fp32", seed=seed)
+    f32.compile(f)
+    f64 = VegasFlow(n_dim, n, verbose=False, precision="fp64", seed=seed, events_limit=n)
+    f64.compile(f)
+    pulls = []
+    for _ in range(4):
+        grid, call = f32.divisions.clone(), f32._call_ctr
+        r32, s32 = (float(v) for v in f32._run_iteration())
+        u = torch.empty((n, n_dim), dtype=torch.float64, device="cuda")
+        nat.call("vf_philox_uniforms", seed, call, call >> 28, 0, n, n_dim, nat.ptr(u), nat.stream_handle())
+        f64.divisions.copy_(grid)
+        f64.set_uniform_source(lambda m, d, u=u: u)
+        r64, s64 = (float(v) for v in f64._run_iteration())
+        assert s32 > 0 and abs(s32 - s64) < 0.02 * s64, (s32, s64)
+        pulls.append((r32 - r64) / s64)
+    print(f"16-D {which} fp32 - fp64 (sigma units): {pulls}")
     assert np.all(np.abs(pulls) < BAR), pulls

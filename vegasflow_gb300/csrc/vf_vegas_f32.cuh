@@ -19,8 +19,10 @@
 //   Gaussian family:    t = (x - mu) sqrt(log2 e) / a as the same affine map,
 //                       f = 2^(-sum t^2)  (the normalisation goes to the float64
 //                       scale)
-//   weight w = prod_d c1 (float32); the constant 50^D xjac (* pref / prod k) is
-//   applied in float64 to the block partials.
+//   weight w = 2^kw prod_d c1 (float32, kw a per-block power-of-two prescale
+//   that keeps a typical event's weight near 1 at any dimension count); the
+//   constant 50^D xjac 2^-kw (* pref / prod k) is applied in float64 to the
+//   block partials.
 //
 // Philox kernel.  A word w stands for the uniform u = (w + 1/2) / 2^32, whose
 // reference bin is trunc(50 (1 - u)) (vflow.py:117, :67).  p = 50 w + 25 is
@@ -194,6 +196,33 @@ __device__ __forceinline__ void f32_bin_affine(const SampleArgs& a, const double
   }
 }
 
+// Binary exponent of |c1| (bounded to float32's normal range; a zero-width bin
+// counts as the smallest), for the weight prescale below.
+__device__ __forceinline__ int f32_cell_exponent(double c1) {
+  const int e = (int)((__double_as_longlong(c1) >> 52) & 0x7FF) - 1023;
+  return e < -126 ? -126 : (e > 127 ? 127 : e);
+}
+
+// The power-of-two prescale of the fp32 weight.  An event's weight prod_d c1
+// can leave float32's range at large dimension counts (prod_d delta ~ 50^-D on
+// a uniform grid: 6.6e-28 at D = 16, whose square underflows), so the kernels
+// accumulate (S w f) and (S w f)^2 with S = 2^k, k = -round(sum_d mean_b
+// log2 |c1_db|) from the cells' binary exponents (`expsum`: their sum over
+// all D x 50 cells): the weight of a typical event -- the bins are equally
+// likely -- is then about 1.  Returns k; the float64 scale takes 2^-k back,
+// so the scaling is exact.
+__device__ __forceinline__ int f32_prescale_exponent(int expsum) {
+  int k = -__float2int_rn((float)expsum / (float)VF_BINS);
+  return k < -100 ? -100 : (k > 100 ? 100 : k);
+}
+
+// Block-wide sum of the per-thread exponent sums into *acc (zeroed before the
+// block's first barrier): a warp reduction, then one shared atomic per warp.
+__device__ __forceinline__ void f32_add_exponents(int* acc, int mine) {
+  mine = __reduce_add_sync(0xffffffffu, mine);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, mine);
+}
+
 // ---- the Philox kernel -------------------------------------------------------
 
 // THREADS: the block size (1024 or 512; the launch-shape autotuner chooses),
@@ -220,21 +249,30 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
 
   // ---- per-block float64 constants; the reversed, replicated table; histograms
   __shared__ double g_mu[D], g_k[D], g_wscale;
+  __shared__ int g_expsum;
+  if (tid == 0) g_expsum = 0;
   f32_block_constants<D, GAUSS, INTEG>(a, g_mu, g_k, &g_wscale, (D & 1) ? -1.0 : 1.0);
+  int expsum = 0;
   for (int k = tid; k < NB; k += THREADS) {
     const int d = k / VF_BINS, b = k - d * VF_BINS;
     double c0, c1;
     f32_bin_affine<GAUSS>(a, g_mu, g_k, d, b, c0, c1);
+    expsum += f32_cell_exponent(c1);
     const float2 cell = make_float2((float)(c0 + 3.0 * c1), (float)(-c1));
     float2* dst = cells + (d * VF_BINS + (VF_BINS - 1 - b)) * VF_F32_TC;
 #pragma unroll
     for (int c = 0; c < VF_F32_TC; ++c) dst[c] = cell;
   }
+  f32_add_exponents(&g_expsum, expsum);
   if (train)
     for (int k = tid; k < vegas_f32_hist_floats(D); k += THREADS) hist[k] = 0.0f;
   __syncthreads();
 
-  const double wscale = g_wscale;  // includes the weight's sign (-1)^D
+  // the weight prescale 2^kw (exact), taken back by the float64 scale, which
+  // also holds the weight's sign (-1)^D
+  const int kw = f32_prescale_exponent(g_expsum);
+  const float wpre = __int_as_float((127 + kw) << 23);
+  const double wscale = g_wscale * ldexp(1.0, -kw);
   [[maybe_unused]] const float wscale_f = (float)wscale;
   IntegrandConsts<float, D> kc;
   if (!GAUSS) load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
@@ -259,7 +297,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
           const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
           const float2 c = *reinterpret_cast<const float2*>(mytab + (jj << 7) + d * DSTRIDE);
           const float t = fmaf(c.y, m, c.x);
-          wf = (d == 0) ? c.y : wf * c.y;
+          wf = (d == 0) ? wpre * c.y : wf * c.y;
           if (GAUSS)
             s = fmaf(t, t, s);
           else
@@ -481,20 +519,27 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __shared__ double g_mu[D], g_k[D], g_wscale;
+  __shared__ int g_expsum;
+  if (tid == 0) g_expsum = 0;
   f32_block_constants<D, GAUSS, INTEG>(a, g_mu, g_k, &g_wscale, 1.0);
+  int expsum = 0;
   for (int k = tid; k < NB; k += THREADS) {
     const int d = k / VF_BINS, b = k - d * VF_BINS;
     double c0, c1;
     f32_bin_affine<GAUSS>(a, g_mu, g_k, d, b, c0, c1);
+    expsum += f32_cell_exponent(c1);
     const float2 cell = make_float2((float)c0, (float)c1);
 #pragma unroll
     for (int c = 0; c < TC; ++c) cells[k * TC + c] = cell;
   }
+  f32_add_exponents(&g_expsum, expsum);
   if (train)
     for (int k = tid; k < inj_hist_bytes(D) / 4; k += THREADS) hist[k] = 0.0f;
   __syncthreads();  // constants, table, histogram and barriers ready
 
-  const double wscale = g_wscale;
+  const int kw = f32_prescale_exponent(g_expsum);  // the weight prescale, as in the Philox kernel
+  const float wpre = __int_as_float((127 + kw) << 23);
+  const double wscale = g_wscale * ldexp(1.0, -kw);
   [[maybe_unused]] const float wscale_f = (float)wscale;
   IntegrandConsts<float, D> kc;
   if (!GAUSS) load_consts<D>(kc, INTEG == VF_INT_USER ? VF_INT_NONE : INTEG, a.params, D);
@@ -522,7 +567,7 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
       }
       const float2 c = *reinterpret_cast<const float2*>(mytab + i * (TC * 8) + d * DSTRIDE);
       const float t = fmaf(c.y, m, c.x);
-      wf = (d == 0) ? c.y : wf * c.y;
+      wf = (d == 0) ? wpre * c.y : wf * c.y;
       if (GAUSS)
         s = fmaf(t, t, s);
       else
