@@ -64,8 +64,8 @@ INSTR_PER_EVENT_FP32_D8 = 208
 INJECTED_BYTES_PER_EVENT = 8 * N_DIM
 
 # DRAM traffic of one fp32 sampler launch (grid, parameters; the partial rows stay
-# in L2), from one ncu capture of a 1e7-event launch: 70.7 KB read, 0 written.
-SAMPLER_DRAM_BYTES = 70656
+# in L2), from one ncu capture of a 1e7-event launch: 40.2 KB read, 0 written.
+SAMPLER_DRAM_BYTES = 40192
 
 
 def _parse():
@@ -509,7 +509,7 @@ def main():
         "fp64_plain": {"value": value64, "unit": "events/s", "ms_per_step": 1e3 * total64 / K,
                        "sampler_ms": 1e3 * float(s64.mean())},
         "fp32_over_fp64": value / value64,
-        "roofline": {"bound": "issue", "kernel": "vf_vegas_f32_kernel<8,SYMGAUSS>",
+        "roofline": {"bound": "issue", "kernel": "vf_vegas_f32_kernel<8,SYMGAUSS,1024>",
                      "achieved": achieved / 1e9, "peak": issue_peak / 1e9, "unit": "Gwarp-instr/s",
                      "frac": achieved / issue_peak, "traffic": SAMPLER_DRAM_BYTES,
                      "traffic_note": "DRAM bytes per launch (ncu dram__bytes_read.sum + "
@@ -612,7 +612,7 @@ def injected_run(dev, n_events, K, W, seed=11):
         "first_timed_iteration": {"mean": float(first[0]), "sigma": float(first[1]),
                                   "pull_vs_exact": (float(first[0]) - exact) / float(first[1])},
         "flags": flags,
-        "roofline": {"bound": "hbm", "kernel": "vf_vegas_f32_kernel<8,SYMGAUSS> (TMA tiles)",
+        "roofline": {"bound": "hbm", "kernel": "vf_vegas_f32_inj_kernel<8,SYMGAUSS> (TMA stage rings)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": INJECTED_BYTES_PER_EVENT * n_events,
                      "traffic_note": "algorithmic bytes; ncu dram__bytes (read + write) on a 1e7-event "

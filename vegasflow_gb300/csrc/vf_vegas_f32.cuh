@@ -105,6 +105,22 @@ __device__ __forceinline__ int joint_cell(int r, int c) {
 // negative, >= 1 -- the caller repeats the float64 operations.  m = 1 + f's top
 // 23 bits (below 1 + the true fraction by less than 2^-23 + 51 2^-32).  About 10
 // 32-bit operations per uniform.  Returns false for the float64 cases.
+// Branch-free form of inj_bin_exact for the fast path of a whole event: ind
+// and m are computed whatever the input (ind stays in 0..49: P < 50 2^32) and
+// the return value says whether they are the reference's; the caller redoes
+// the event's failing uniforms (rare) with the exact operations.
+__device__ __forceinline__ bool inj_bin_fast(u64 bits, int& ind, float& m) {
+  const u32 bh = (u32)(bits >> 32), bl = (u32)bits;
+  const u32 sh = (bh >> 20) - 1011u;
+  const u32 mh = (bh & 0xFFFFFu) | 0x100000u;
+  const u32 h = __funnelshift_l(bl, mh, sh);
+  const u64 P = (u64)(~h) * 50ull;
+  const u32 f = (u32)P;
+  ind = (int)(P >> 32);
+  m = __uint_as_float(__funnelshift_r(f, 0x7Fu, 9));
+  return (sh <= 11u) & (f - 1u < 0xFFFFFFCCu);
+}
+
 __device__ __forceinline__ bool inj_bin_exact(u64 bits, int& ind, float& m) {
   const u32 bh = (u32)(bits >> 32), bl = (u32)bits;
   const u32 sh = (bh >> 20) - 1011u;  // biased exponent - 1011: u in [2^-12, 1) <=> sh in [0, 11]
@@ -547,24 +563,30 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
   F2 s1 = {0.0f, 0.0f}, s2 = {0.0f, 0.0f};
   int bad = 0;
 
-  auto event = [&](const u64 (&ub)[D], long long e) {
-    int bins[D];
-    float x[D];
-    float wf = 1.0f, s = 0.0f;
+  // the bin and fraction of one uniform exactly (the rare cases of the integer
+  // map: the reference's float64 operations, vflow.py:117, :67)
+  auto exact_bin = [&](u64 ub, int& i, float& m) {
+    if (!inj_bin_exact(ub, i, m)) {
+      const double xn = __dmul_rn(50.0, __dsub_rn(1.0, __longlong_as_double((long long)ub)));
+      i = (int)xn;
+      if (i < 0 || i > VF_BINS - 1) {
+        bad = 1;
+        i = i < 0 ? 0 : VF_BINS - 1;
+      }
+      m = (float)(1.0 + (xn - floor(xn)));
+    }
+  };
+  // the event's dimensions through the table, the bins from `bin_of` (fast or
+  // exact); returns whether every bin came out exact (always, for the exact one)
+  auto map_dims = [&](const u64 (&ub)[D], int (&bins)[D], float& wf, float& s, float (&x)[D], auto bin_of) {
+    bool ok = true;
+    wf = 1.0f;
+    s = 0.0f;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       int i;
       float m;
-      if (!inj_bin_exact(ub[d], i, m)) {
-        // the bin in float64, bit-exact with the reference (vflow.py:117, :67)
-        const double xn = __dmul_rn(50.0, __dsub_rn(1.0, __longlong_as_double((long long)ub[d])));
-        i = (int)xn;
-        if (i < 0 || i > VF_BINS - 1) {
-          bad = 1;
-          i = i < 0 ? 0 : VF_BINS - 1;
-        }
-        m = (float)(1.0 + (xn - floor(xn)));
-      }
+      ok &= bin_of(ub[d], i, m);
       const float2 c = *reinterpret_cast<const float2*>(mytab + i * (TC * 8) + d * DSTRIDE);
       const float t = fmaf(c.y, m, c.x);
       wf = (d == 0) ? wpre * c.y : wf * c.y;
@@ -574,6 +596,21 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
         x[d] = t;
       bins[d] = i;
     }
+    return ok;
+  };
+
+  auto event = [&](const u64 (&ub)[D], long long e) {
+    int bins[D];
+    float x[D];
+    float wf, s;
+    // every uniform by the integer map, one check for the event; an event with
+    // a uniform the map cannot decide (about one in 1e7 at D = 8 on U[0, 1)
+    // uniforms) is mapped again with the exact operations
+    if (!map_dims(ub, bins, wf, s, x, [](u64 b, int& i, float& m) { return inj_bin_fast(b, i, m); }))
+      map_dims(ub, bins, wf, s, x, [&](u64 b, int& i, float& m) {
+        exact_bin(b, i, m);
+        return true;
+      });
     float f;
     if constexpr (GAUSS) {
       f = ex2_approx_ftz(-s);
@@ -632,6 +669,7 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
         u64 ub[D];
 #pragma unroll
         for (int j = 0; j < D / 2; ++j) {
+          // this thread's row, 16 bytes at a time, at the tensor map's swizzled offsets
           const u32 off = (u32)(r * ROWB + 16 * j);
           const u32 addr = stage + (off ^ (((off >> 7) & swz) << 4));
           asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(ub[2 * j]), "=l"(ub[2 * j + 1]) : "r"(addr));
