@@ -64,11 +64,13 @@ __host__ __device__ inline int batch_smem_bytes(int max_dim) {
   return max_dim * VF_BINS * 8 + vegas_f32_joint_floats(max_dim) * 4;
 }
 
-// Stage one integral (table cells, weight constant) in shared memory.
+// Stage one integral (table cells, weight constant) in shared memory; the
+// cells' binary exponents go into *expsum (zeroed by the caller before this
+// function's first barrier) for the weight prescale (f32_prescale_exponent).
 template <int D, bool GAUSS>
 __device__ __forceinline__ double batch_stage(const BatchItem& it, const double* __restrict__ grids,
                                               const double* __restrict__ params, float2* cells,
-                                              double* g_mu, double* g_k) {
+                                              double* g_mu, double* g_k, int* expsum) {
   constexpr double SQRT_LOG2E = 1.2011224087864498;
   const double* grid = grids + it.grid_off;
   const double* p = params + it.param_off;
@@ -78,6 +80,7 @@ __device__ __forceinline__ double batch_stage(const BatchItem& it, const double*
     g_k[tid] = SQRT_LOG2E / (it.integrand == VF_INT_SYMGAUSS ? p[0] : p[D + tid]);
   }
   __syncthreads();
+  int mine = 0;
   for (int k = tid; k < D * VF_BINS; k += blockDim.x) {
     const int d = k / VF_BINS, b = k - d * VF_BINS;
     const double lo = grid[d * VF_EDGES + b];
@@ -87,8 +90,10 @@ __device__ __forceinline__ double batch_stage(const BatchItem& it, const double*
       c0 = (c0 - g_mu[d]) * g_k[d];
       c1 = c1 * g_k[d];
     }
+    mine += f32_cell_exponent(c1);
     cells[k] = make_float2((float)c0, (float)c1);
   }
+  f32_add_exponents(expsum, mine);
   double ws = it.xjac;
   for (int d = 0; d < D; ++d) ws *= 50.0;
   if (GAUSS) {
@@ -110,14 +115,19 @@ __device__ void batch_tile(const BatchArgs& a, const BatchItem& it, int tile, bo
   float* hist = reinterpret_cast<float*>(smem + a.max_dim * VF_BINS * 8);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool train = it.train != 0;
+  __shared__ int s_expsum;  // the staged integral's cell exponents (kept until the next restage)
   if (restage) {
-    const double ws = batch_stage<D, GAUSS>(it, a.grids, a.params, cells, g_mu, g_k);
+    if (tid == 0) s_expsum = 0;
+    const double ws = batch_stage<D, GAUSS>(it, a.grids, a.params, cells, g_mu, g_k, &s_expsum);
     if (tid == 0) *s_wscale = ws;
   }
   if (train)
     for (int k = tid; k < NP * 2500 + (D & 1) * VF_BINS; k += blockDim.x) hist[k] = 0.0f;
   __syncthreads();
-  const double wscale = *s_wscale;
+  // the weight prescale 2^kw of the fp32 samplers (exact; the float64 scale takes it back)
+  const int kw = f32_prescale_exponent(s_expsum);
+  const float wpre = __int_as_float((127 + kw) << 23);
+  const double wscale = *s_wscale * ldexp(1.0, -kw);
   const float wscale_f = (float)wscale;  // the full weight handed to a user integrand
   const double* iparams = a.params + it.param_off;
   IntegrandConsts<float, D> kc;
@@ -146,7 +156,7 @@ __device__ void batch_tile(const BatchArgs& a, const BatchItem& it, int tile, bo
           const float m = __uint_as_float(((u32)pp >> 9) | 0x3F800000u);
           const float2 c = cells[d * VF_BINS + i];
           const float t = fmaf(c.y, m, c.x);
-          wf = (d == 0) ? c.y : wf * c.y;
+          wf = (d == 0) ? wpre * c.y : wf * c.y;
           if (GAUSS)
             s = fmaf(t, t, s);
           else

@@ -493,10 +493,6 @@ __host__ __device__ inline int vegas_f32_inj_smem_bytes(int D, int train, bool t
   return base + 1024 + VF_INJ_GROUPS * inj_stages(D) * inj_tile_bytes(D);
 }
 
-__device__ __forceinline__ void named_sync(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
 // All threads of named barrier `id` (count threads) vote: whether every one has `ok`.
 __device__ __forceinline__ bool named_all(int id, int count, bool ok) {
   u32 r;
@@ -576,9 +572,9 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
       m = (float)(1.0 + (xn - floor(xn)));
     }
   };
-  // the event's dimensions through the table, the bins from `bin_of` (fast or
-  // exact); returns whether every bin came out exact (always, for the exact one)
-  auto map_dims = [&](const u64 (&ub)[D], int (&bins)[D], float& wf, float& s, float (&x)[D], auto bin_of) {
+  // the event's dimensions through the table, the bins by the fast integer map
+  // or (`exact`) the exact one; returns whether every bin came out exact
+  auto map_dims = [&](const u64 (&ub)[D], int (&bins)[D], float& wf, float& s, float (&x)[D], bool exact) {
     bool ok = true;
     wf = 1.0f;
     s = 0.0f;
@@ -586,7 +582,10 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
     for (int d = 0; d < D; ++d) {
       int i;
       float m;
-      ok &= bin_of(ub[d], i, m);
+      if (exact)
+        exact_bin(ub[d], i, m);
+      else
+        ok &= inj_bin_fast(ub[d], i, m);
       const float2 c = *reinterpret_cast<const float2*>(mytab + i * (TC * 8) + d * DSTRIDE);
       const float t = fmaf(c.y, m, c.x);
       wf = (d == 0) ? wpre * c.y : wf * c.y;
@@ -606,11 +605,7 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
     // every uniform by the integer map, one check for the event; an event with
     // a uniform the map cannot decide (about one in 1e7 at D = 8 on U[0, 1)
     // uniforms) is mapped again with the exact operations
-    if (!map_dims(ub, bins, wf, s, x, [](u64 b, int& i, float& m) { return inj_bin_fast(b, i, m); }))
-      map_dims(ub, bins, wf, s, x, [&](u64 b, int& i, float& m) {
-        exact_bin(b, i, m);
-        return true;
-      });
+    if (!map_dims(ub, bins, wf, s, x, false)) map_dims(ub, bins, wf, s, x, true);
     float f;
     if constexpr (GAUSS) {
       f = ex2_approx_ftz(-s);
@@ -662,10 +657,6 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
         const int st = k % STAGES;
         const u32 stage = stage0 + (u32)st * TILEB;
         const bool ok = mbar_wait_bounded(smem_u32(&tma_bar[g][st]), (u32)((k / STAGES) & 1));
-        if (!named_all(1 + g, VF_INJ_ROWS, ok)) {  // a copy never completed: report, stop this group
-          if (r == 0 && a.flags) atomicOr(a.flags, VF_FLAG_TIMEOUT);
-          break;
-        }
         u64 ub[D];
 #pragma unroll
         for (int j = 0; j < D / 2; ++j) {
@@ -674,7 +665,14 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
           const u32 addr = stage + (off ^ (((off >> 7) & swz) << 4));
           asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(ub[2 * j]), "=l"(ub[2 * j + 1]) : "r"(addr));
         }
-        named_sync(1 + g, VF_INJ_ROWS);  // the stage is read: refill it while the events are evaluated
+        // one barrier of the group both says the stage is read (it can be
+        // refilled while the events are evaluated) and votes on the wait: if a
+        // copy never completed, the rows just read are discarded and the group
+        // reports and stops
+        if (!named_all(1 + g, VF_INJ_ROWS, ok)) {
+          if (r == 0 && a.flags) atomicOr(a.flags, VF_FLAG_TIMEOUT);
+          break;
+        }
         if (r == 0 && t + STAGES * step < n_tiles) {
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           tma_load_tile(stage, a.tmap, 0, (int)((t + STAGES * step) * VF_INJ_ROWS), smem_u32(&tma_bar[g][st]),
