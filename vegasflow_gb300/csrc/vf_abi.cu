@@ -413,7 +413,7 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
   if (fast) {
     a.hist_copies = 0;
     if (inj) {
-      // injected uniforms: TMA tiles of VF_INJ_ROWS rows into each group's
+      // injected uniforms: TMA tiles of VF_INJ_ROWS rows into each warp's
       // stage ring when the array allows it
       a.tma_swizzle = encode_uniform_tiles(a, u_inj, n_events, n_dim, VF_INJ_ROWS);
       smem = vf::vegas_f32_inj_smem_bytes(n_dim, a.train, a.tma_swizzle != 0);

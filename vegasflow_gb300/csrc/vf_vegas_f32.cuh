@@ -447,22 +447,22 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
 //
 // Injected float64 uniforms ([n][D] row-major, streamed once) with the
 // reference's float64 bin of every uniform (inj_bin_exact, or the float64
-// operations in its rare cases).  1024 threads per block (one block per SM) in
-// VF_INJ_GROUPS groups of VF_INJ_ROWS threads.  With a.tma_swizzle set (D = 4,
-// 8, 16 and a 16-byte aligned array) each group streams its own tiles of
-// VF_INJ_ROWS events (thread r of the group takes row r) through a ring of
-// `stages` shared-memory stages filled by TMA tensor copies (the tensor map's
-// 32/64/128-byte swizzle makes every quarter-warp read of a row
-// conflict-free): a thread copies its row to registers, the group meets at its
-// named barrier, its first thread issues the copy of the tile `stages` ahead
-// into the freed stage, and the events are evaluated while the copies land --
-// four groups keep up to 4 `stages` tiles in flight per SM.  Otherwise plain
-// loads (16-byte, evict-first when D is even and the array is aligned).
+// operations in its rare cases).  1024 threads per block (one block per SM).
+// With a.tma_swizzle set (D = 4, 8, 16 and a 16-byte aligned array) every warp
+// streams its own tiles of VF_INJ_ROWS = 32 events (lane r takes row r)
+// through a ring of `stages` shared-memory stages filled by TMA tensor copies
+// (the tensor map's 32/64/128-byte swizzle makes every quarter-warp read of a
+// row conflict-free): the lanes copy their rows to registers, meet at a warp
+// barrier that also votes on the wait, lane 0 issues the copy of the tile
+// `stages` ahead into the freed stage, and the events are evaluated while the
+// copies land -- 32 warps keep up to 32 `stages` tiles (64-128 KB) in flight
+// per SM, and no warp waits for another.  Otherwise plain loads (16-byte,
+// evict-first when D is even and the array is aligned).
 // The bin table is lane-replicated as in the Philox kernel but in bin order,
 // the histogram joint pair tables have 50-float rows.
 
 #define VF_INJ_THREADS 1024
-#define VF_INJ_ROWS 256
+#define VF_INJ_ROWS 32
 #define VF_INJ_GROUPS (VF_INJ_THREADS / VF_INJ_ROWS)
 #define VF_SMEM_LIMIT 232448  // dynamic shared memory a block may use (227 KB)
 
@@ -493,17 +493,6 @@ __host__ __device__ inline int vegas_f32_inj_smem_bytes(int D, int train, bool t
   return base + 1024 + VF_INJ_GROUPS * inj_stages(D) * inj_tile_bytes(D);
 }
 
-// All threads of named barrier `id` (count threads) vote: whether every one has `ok`.
-__device__ __forceinline__ bool named_all(int id, int count, bool ok) {
-  u32 r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}"
-      : "=r"(r)
-      : "r"((u32)ok), "r"(id), "r"(count)
-      : "memory");
-  return r != 0;
-}
-
 template <int D, int INTEG, bool TAP = false>
 __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(const __grid_constant__ SampleArgs a) {
   constexpr int THREADS = VF_INJ_THREADS;
@@ -521,7 +510,7 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
   const int warp = tid >> 5;
   const bool train = a.train != 0;
 
-  // the TMA path's barriers: one per stage of every group, initialised before
+  // the TMA path's barriers: one per stage of every warp, initialised before
   // the block-wide sync below
   __shared__ alignas(8) u64 tma_bar[VF_INJ_GROUPS][STAGES > 0 ? STAGES : 1];
   const bool tma = STAGES > 0 && a.tma_swizzle != 0;
@@ -636,12 +625,12 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
   if constexpr (STAGES > 0) {
     if (tma) {
       constexpr int ROWB = 8 * D;
-      constexpr u32 TILEB = inj_tile_bytes(D);  // a multiple of 1024
+      constexpr u32 TILEB = inj_tile_bytes(D);  // 1, 2 or 4 KB: every stage on a 1 KB boundary
       const u32 ring = (smem_u32(smem) + (u32)vegas_f32_inj_smem_bytes(D, a.train) + 1023u) & ~1023u;
-      const int g = tid / VF_INJ_ROWS, r = tid % VF_INJ_ROWS;
+      const int g = warp, r = lane;
       const u32 stage0 = ring + (u32)(g * STAGES) * TILEB;
       const long long n_tiles = (n + VF_INJ_ROWS - 1) / VF_INJ_ROWS;
-      // the group's tiles: first, first + step, ...
+      // the warp's tiles: first, first + step, ...
       const long long step = (long long)gridDim.x * VF_INJ_GROUPS;
       const long long first = (long long)blockIdx.x * VF_INJ_GROUPS + g;
       if (r == 0)
@@ -665,11 +654,13 @@ __global__ void __launch_bounds__(VF_INJ_THREADS, 1) vf_vegas_f32_inj_kernel(con
           const u32 addr = stage + (off ^ (((off >> 7) & swz) << 4));
           asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(ub[2 * j]), "=l"(ub[2 * j + 1]) : "r"(addr));
         }
-        // one barrier of the group both says the stage is read (it can be
-        // refilled while the events are evaluated) and votes on the wait: if a
-        // copy never completed, the rows just read are discarded and the group
+        // one warp barrier both says the stage is read (it can be refilled
+        // while the events are evaluated) and votes on the wait: if a copy
+        // never completed, the rows just read are discarded and the warp
         // reports and stops
-        if (!named_all(1 + g, VF_INJ_ROWS, ok)) {
+        const bool all_ok = __all_sync(0xffffffffu, ok);
+        __syncwarp();
+        if (!all_ok) {
           if (r == 0 && a.flags) atomicOr(a.flags, VF_FLAG_TIMEOUT);
           break;
         }
