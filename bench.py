@@ -665,7 +665,7 @@ def sampler_run(dev, n_events, K, W, seed=3):
     return {
         "workload": f"generate_random_array({n_events:.0e}) on a trained {N_DIM}-D grid, fp32 x and weight",
         "value": n_events / (api_ms / 1e3), "unit": "events/s", "ms_per_call": api_ms, "kernel_ms": kern_ms,
-        "roofline": {"bound": "hbm", "kernel": "vf_vegas_f32_map_kernel<8>", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "vf_vegas_f32_map_kernel<8,false>", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": bytes_per_event * n_events,
                      "traffic_note": "algorithmic bytes written (x 32 B + w 4 B per event)",
                      "peak_source": source},

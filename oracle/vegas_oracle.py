@@ -31,11 +31,11 @@ __all__ = [
     "words_to_u53", "vegas_map", "plus_map", "importance_sampling_digest",
     "consume_array_into_indices", "refine_grid_per_dimension", "refine_grid",
     "initial_grid", "plus_stratification", "redistribute_samples",
-    "weighted_average", "chunk_sizes", "vegas_map_f32_words", "plain_map_f32_words",
+    "weighted_average", "chunk_sizes", "vegas_map_f32_words", "f32_weight_prescale", "plain_map_f32_words",
     "OracleVegas", "OraclePlain", "OraclePlus", "INTEGRANDS", "integrand_symgauss",
     "integrand_gauss_mu", "integrand_breit_wigner", "integrand_prod", "integrand_sum",
     "symgauss_exact", "gauss_mu_exact", "breit_wigner_exact", "threaded_vegas_iteration",
-    "vegas_f32_table", "uniforms_of_words", "plus_bins_from_words", "hypercube_points",
+    "uniforms_of_words", "plus_bins_from_words", "hypercube_points",
     "fma_f32",
 ]
 
@@ -546,46 +546,63 @@ def fma_f32(a, b, c):
     return s.astype(np.float32)
 
 
-def vegas_f32_table(divisions):
-    """The per-bin table {c0, c1} of the fp32 VEGAS samplers without integration
-    limits: ``c1 = delta``, ``c0 = lo - delta``, each computed in float64 from the
-    grid and rounded once to float32 (so that ``x = c0 + c1 m`` for m in [1, 2))."""
-    g = np.asarray(divisions, dtype=np.float64)
-    lo = g[:, :-1]
-    dl = g[:, 1:] - lo
-    return (lo - dl).astype(np.float32), dl.astype(np.float32)
+def f32_weight_prescale(c1):
+    """Exponent k of the fp32 samplers' power-of-two weight prescale 2^k for the
+    float64 bin widths ``c1`` (any shape, all D x 50 cells): the sum of their
+    binary exponents, each clamped to float32's normal range [-126, 127] (a zero
+    width counts as -126), divided by 50 in float32, rounded to the nearest
+    integer (ties to even), negated and clamped to [-100, 100]."""
+    bits = np.asarray(c1, dtype=np.float64).view(np.uint64)
+    e = ((bits >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64) - 1023
+    expsum = int(np.clip(e, -126, 127).sum())
+    k = -int(np.rint(np.float32(expsum) / np.float32(BINS_MAX)))
+    return max(-100, min(100, k))
 
 
 def vegas_map_f32_words(words, divisions, xjac):
     """fp32 form of the importance map on one 32-bit Philox word per dimension
     (the fused sampler's and the map kernel's draw, no integration limits).
 
-    With t = (~word + 1/2) / 2^32 standing for ``1 - u``, u = (word + 1/2) / 2^32:
-    ``p = 50 * ~word + 25`` (exact, 64-bit) is 50 t 2^32, so ``ind = p >> 32`` is
-    the reference's ``int32(50 (1 - u))`` (vflow.py:117, :67; exact in float64 for
-    such u) and ``m = 1 + (top 23 bits of p mod 2^32) / 2^23`` its fraction plus 1.
-    ``x = fl32(c1 m + c0)`` (one fused multiply-add through the table of
-    ``vegas_f32_table``), ``w = prod_d c1`` in float32 left to right, times the
-    float32 constant ``xjac * 50^n_dim`` (its float64 product rounded once).
+    With u = (word + 1/2) / 2^32: ``p = 50 * word + 25`` (exact, 64-bit) is
+    50 u 2^32, so ``j = p >> 32`` is floor(50 u) and ``ind = 49 - j`` the
+    reference's ``int32(50 (1 - u))`` (vflow.py:117, :67; exact in float64 for
+    such u); ``m = 1 + (top 23 bits of p mod 2^32) / 2^23`` is 1 + frac(50 u).
+    The table is reversed: with c0 = lo - delta and c1 = delta (float64), the
+    cell of bin b holds ``C0 = f32(fma64(3, c1, c0))`` and ``C1 = f32(-c1)``, so
+    that ``x = fl32(C1 m + C0)`` (one fused multiply-add) is
+    lo + delta (1 - frac(50 u)), the reference's lo + delta frac.  The weight is
+    2^k C1_0 C1_1 ... C1_{D-1} in float32 left to right (k from
+    ``f32_weight_prescale``) times the float32 constant
+    ``(-1)^D xjac 50^D 2^-k`` (its float64 product rounded once).
     Returns (ind int32, x float32, w float32)."""
+    from fractions import Fraction
     words = np.asarray(words, dtype=np.uint32)
     n, n_dim = words.shape
-    inv = (~words).astype(np.uint64)
-    p = inv * np.uint64(50) + np.uint64(25)
-    ind = (p >> np.uint64(32)).astype(np.int32)
+    p = words.astype(np.uint64) * np.uint64(50) + np.uint64(25)
+    j = (p >> np.uint64(32)).astype(np.int32)
+    ind = (BINS_MAX - 1 - j).astype(np.int32)
     mbits = ((p & _MASK32) >> np.uint64(9)).astype(np.uint32) | np.uint32(0x3F800000)
     m = mbits.view(np.float32)
-    c0, c1 = vegas_f32_table(divisions)
-    c0e = np.take_along_axis(c0, ind.T, axis=1).T
-    c1e = np.take_along_axis(c1, ind.T, axis=1).T
+    g = np.asarray(divisions, dtype=np.float64)
+    lo = g[:, :-1]
+    c1 = g[:, 1:] - lo
+    c0 = lo - c1
+    # fma64(3, c1, c0) rounded to float64 once (exact rational sum, nearest-even)
+    big = np.array([[float(Fraction(3) * Fraction(float(b)) + Fraction(float(a))) for a, b in zip(ra, rb)]
+                    for ra, rb in zip(c0, c1)])
+    C0 = big.astype(np.float32)
+    C1 = (-c1).astype(np.float32)
+    c0e = np.take_along_axis(C0, ind.T, axis=1).T
+    c1e = np.take_along_axis(C1, ind.T, axis=1).T
     x = fma_f32(c1e, m, c0e)
-    wf = c1e[:, 0].copy()
+    k = f32_weight_prescale(c1)
+    wf = (np.float32(2.0 ** k) * c1e[:, 0]).astype(np.float32)
     for d in range(1, n_dim):
         wf = (wf * c1e[:, d]).astype(np.float32)
-    ws = float(xjac)
+    ws = -float(xjac) if n_dim & 1 else float(xjac)
     for _ in range(n_dim):
         ws *= 50.0
-    w = (wf * np.float32(ws)).astype(np.float32)
+    w = (wf * np.float32(ws * 2.0 ** -k)).astype(np.float32)
     return ind, x, w
 
 

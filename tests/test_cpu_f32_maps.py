@@ -48,7 +48,23 @@ def test_vegas_f32_bins_are_the_reference_bins():
         lo = np.take_along_axis(grid, ind.T, axis=1).T
         hi = np.take_along_axis(grid, ind.T + 1, axis=1).T
         assert np.all(x >= lo - 1e-6) and np.all(x <= hi + 1e-6)
-        assert np.all(w > 0)
+        # the weight is the float64 weight within float32 rounding (D + 2 roundings)
+        w64 = np.prod(hi - lo, axis=1) * 50.0 ** n_dim / words.shape[0]
+        np.testing.assert_allclose(w, w64, rtol=(n_dim + 2) * 2.0 ** -23)
+
+
+def test_f32_weight_prescale_keeps_16d_weights_in_range():
+    """Narrow bins at 16 dimensions: prod_d delta underflows float32 without the
+    power-of-two prescale, with it the weight keeps float32 precision."""
+    n_dim = 16
+    edges = np.concatenate([[0.0], np.linspace(0.001, 1.0, 50)])  # bin 0 is 0.001 wide
+    grid = np.tile(edges, (n_dim, 1))
+    words = np.full((4, n_dim), 0xFFFFFFFF, dtype=np.uint32)  # u -> 1: bin 0 in every dimension
+    ind, _, w = oracle.vegas_map_f32_words(words, grid, 1.0)
+    assert np.all(ind == 0)
+    w64 = 0.001 ** n_dim * 50.0 ** n_dim
+    assert np.float32(0.001) ** n_dim == 0.0  # the plain float32 product underflows
+    np.testing.assert_allclose(w, w64, rtol=18 * 2.0 ** -23)
 
 
 def test_plus_f32_bins_are_the_reference_bins():

@@ -56,25 +56,27 @@ def test_fused_sampler_bins_are_the_reference_bins(n_dim, which, offset):
     np.testing.assert_array_equal(ind.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("n_dim", [1, 3, 8, 16])
-def test_map_kernel_points_and_weights_match_oracle(n_dim):
-    n, call = 1_000_000, 5
+@pytest.mark.parametrize("n_dim", [1, 3, 5, 8, 16])
+@pytest.mark.parametrize("with_ind", [True, False])
+def test_map_kernel_points_and_weights_match_oracle(n_dim, with_ind):
+    """x, w (and bins) of the map kernel bit for bit against the oracle's
+    restatement; n is not a multiple of the 32-event tiles, so the last tile
+    takes the plain-store path."""
+    n, call = 1_000_003, 5
     inst = _trained(n_dim, n, integrands.symgauss(0.2))
     x = torch.empty((n, n_dim), dtype=torch.float32, device="cuda")
     w = torch.empty(n, dtype=torch.float32, device="cuda")
-    ind = torch.empty((n, n_dim), dtype=torch.int32, device="cuda")
+    ind = torch.empty((n, n_dim), dtype=torch.int32, device="cuda") if with_ind else None
     inst._sample(n, 0, call, nat.VF_INT_NONE, None, False, False, ind=ind, x=x, w=w)
     torch.cuda.synchronize()
     words = oracle.philox_words(inst._seed, call, 0, n, n_dim)
     grid = inst.divisions.cpu().numpy()
     ind_o, x_o, w_o = oracle.vegas_map_f32_words(words, grid, inst.xjac)
-    np.testing.assert_array_equal(ind.cpu().numpy(), ind_o)
+    if with_ind:
+        np.testing.assert_array_equal(ind.cpu().numpy(), ind_o)
     np.testing.assert_array_equal(ind_o, _reference_bins(oracle.uniforms_of_words(words), grid))
-    xg = x.cpu().numpy()
-    assert np.all(xg >= 0) and np.all(x_o >= 0)  # the int32 views of non-negative floats are ordered
-    ulps = np.abs(xg.view(np.int32).astype(np.int64) - x_o.view(np.int32).astype(np.int64))
-    assert ulps.max() <= 1, ulps.max()
-    np.testing.assert_array_equal(w.cpu().numpy(), w_o)
+    np.testing.assert_array_equal(x.cpu().numpy().view(np.uint32), x_o.view(np.uint32))
+    np.testing.assert_array_equal(w.cpu().numpy().view(np.uint32), w_o.view(np.uint32))
 
 
 def _near_edge_uniforms(n_dim):

@@ -243,7 +243,10 @@ int vf_preload(void) {
       load(vf::vegas_f32_inj_kernel(d, integ, true));
     }
   }
-  for (int d = 1; d <= VF_MAX_DIM; ++d) load(vf::vegas_f32_map_kernel(d));
+  for (int d = 1; d <= VF_MAX_DIM; ++d) {
+    load(vf::vegas_f32_map_kernel(d, false));
+    load(vf::vegas_f32_map_kernel(d, true));
+  }
   for (int dmax : {4, 8, 16})
     for (int integ = VF_INT_NONE; integ <= VF_INT_SUM; ++integ) {
       load(vf::sample_kernel_f64(dmax, integ));
@@ -381,20 +384,22 @@ int sample_impl(int alg, int precision, const double* grid, int n_dim, long long
   a.call_dev = call_dev;
   fill_philox(a, seed, call_ctr);
   if (map_only) {
-    const void* km = vf::vegas_f32_map_kernel(n_dim);
+    const bool with_ind = ind_out != nullptr;
+    const void* km = vf::vegas_f32_map_kernel(n_dim, with_ind);
     if (!km) return fail(VF_ERR_UNSUPPORTED, "vf_sample: no map kernel for n_dim=%d", n_dim);
-    const int smem_m = vf::vegas_f32_map_smem_bytes(n_dim, VF_THREADS, ind_out != nullptr);
+    const int smem_m = vf::vegas_f32_map_smem_bytes(n_dim, with_ind);
     int rc = prepare_smem(km, smem_m);
     if (rc) return rc;
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, km, VF_THREADS, smem_m) != cudaSuccess || per_sm < 1)
-      return fail(VF_ERR_CUDA, "vf_sample: occupancy query for the map kernel failed");
-    const long long tiles = (n_events + VF_MAP_EPT * VF_THREADS - 1) / (VF_MAP_EPT * VF_THREADS);
-    long long blocks_m = (long long)per_sm * sm_count();
-    if (tiles < blocks_m) blocks_m = tiles > 0 ? tiles : 1;
+    const int fit = resident_blocks(km, VF_MAP_THREADS, smem_m);
+    if (fit < 1) return fail(VF_ERR_CUDA, "vf_sample: occupancy query for the map kernel failed");
+    // one 32-event tile per warp at least: no more blocks than the tiles need
+    const long long per_block = 32LL * vf::map_ept(n_dim, with_ind) * (VF_MAP_THREADS / 32);
+    const long long need = (n_events + per_block - 1) / per_block;
+    long long blocks_m = fit;
+    if (need < blocks_m) blocks_m = need > 0 ? need : 1;
     void* args[] = {&a};
     const cudaError_t e =
-        cudaLaunchKernel(km, dim3((unsigned)blocks_m), dim3(VF_THREADS), args, smem_m, (cudaStream_t)stream);
+        cudaLaunchKernel(km, dim3((unsigned)blocks_m), dim3(VF_MAP_THREADS), args, smem_m, (cudaStream_t)stream);
     if (e != cudaSuccess) return fail(VF_ERR_LAUNCH, "vf_sample launch: %s", cudaGetErrorString(e));
     return check_launch("vf_sample (map)");
   }

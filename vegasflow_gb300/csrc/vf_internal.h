@@ -48,9 +48,9 @@ const void* plus_f32_kernel(int n_dim, int integrand);
 // VF_INT_SYMGAUSS and VF_INT_BREIT_WIGNER, dimensions 1..16.
 const void* plus_f32_tap_kernel(int n_dim, int integrand);
 
-// The fp32 VEGAS map kernel without an integrand (x, w, bin indices to HBM),
-// specialised on the dimension count; 256 threads per block.
-const void* vegas_f32_map_kernel(int n_dim);
+// The fp32 VEGAS map kernel without an integrand (x, w and, with `ind`, bin
+// indices to HBM), specialised on the dimension count; VF_MAP_THREADS per block.
+const void* vegas_f32_map_kernel(int n_dim, bool ind);
 
 // Launches the NVRTC-compiled sampler of a JIT integrand with `args` (a
 // SampleArgs); reports whether it is the fp32 VEGAS kernel and settles the

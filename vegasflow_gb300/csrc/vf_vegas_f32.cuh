@@ -203,7 +203,7 @@ __device__ __forceinline__ void f32_bin_affine(const SampleArgs& a, const double
   c0 = lo - dl;
   c1 = dl;
   if (a.xmin != nullptr) {
-    c0 = a.xmin[d] + c0 * a.xdelta[d];
+    c0 = __fma_rn(c0, a.xdelta[d], a.xmin[d]);
     c1 = c1 * a.xdelta[d];
   }
   if (GAUSS) {
@@ -274,7 +274,7 @@ vf_vegas_f32_kernel(const __grid_constant__ SampleArgs a) {
     double c0, c1;
     f32_bin_affine<GAUSS>(a, g_mu, g_k, d, b, c0, c1);
     expsum += f32_cell_exponent(c1);
-    const float2 cell = make_float2((float)(c0 + 3.0 * c1), (float)(-c1));
+    const float2 cell = make_float2((float)__fma_rn(3.0, c1, c0), (float)(-c1));
     float2* dst = cells + (d * VF_BINS + (VF_BINS - 1 - b)) * VF_F32_TC;
 #pragma unroll
     for (int c = 0; c < VF_F32_TC; ++c) dst[c] = cell;
