@@ -57,6 +57,30 @@ def test_map_events_are_the_fused_samplers_events():
     assert abs(res_torch - res_fused) <= 2e-5 * abs(res_fused)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("plus", [False, True])
+def test_generate_random_array_normalisation_folded(precision, plus):
+    """generate_random_array writes w already normalised (the Jacobian given to
+    the sampler is xjac / (xjac n)); the same events through the raw sampler,
+    divided as the reference divides (monte_carlo.py:245; vflowplus.py:182-183),
+    agree to the precision's rounding."""
+    from vegasflow_gb300 import VegasFlowPlus
+    n_it, n = 200_000, 150_000
+    inst = (VegasFlowPlus(3, n_it, verbose=False, precision=precision, seed=4) if plus
+            else VegasFlow(3, n_it, verbose=False, precision=precision, seed=4))
+    inst.compile(integrands.symgauss(0.3))
+    inst.run_integration(2)
+    ctr = inst._call_ctr
+    x, p = inst.generate_random_array(n)
+    inst._call_ctr = ctr
+    xr, wr, *_ = inst._generate_random_array(n_it if plus else n)
+    want = wr[:n] / (inst.xjac * n_it) * n_it / n if plus else wr / (inst.xjac * n)
+    assert tuple(p.shape) == (n,) and p.dtype == want.dtype
+    torch.testing.assert_close(x, xr[:n], rtol=0, atol=0)
+    rtol = 4 * float(torch.finfo(p.dtype).eps)
+    torch.testing.assert_close(p, want, rtol=rtol, atol=0)
+
+
 def test_generate_random_array_weights():
     """generate_random_array's weights integrate the constant 1: sum over the
     events of xjac (= Jacobian / n) estimates the volume of the unit cube."""

@@ -311,11 +311,12 @@ class MonteCarloFlow(ABC):
 
     # ---------------------------------------------------------------- sampling
     def _sample(self, n_events, ev_offset, call, integrand_id, params, train, accumulate,
-                u_inj=None, ind=None, x=None, w=None, f=None):
+                u_inj=None, ind=None, x=None, w=None, f=None, xjac=None):
         ws = self._workspace()
         xmin, xdelta, xdj = self._limits_ptrs()
+        xjac = self.xjac if xjac is None else xjac
         nat.call("vf_sample", self._ALG, self._prec, self._grid_ptr(), self.n_dim, int(n_events),
-                 int(ev_offset), float(self.xjac), xmin, xdelta, float(xdj), nat.ptr(u_inj),
+                 int(ev_offset), float(xjac), xmin, xdelta, float(xdj), nat.ptr(u_inj),
                  self._seed, call, int(integrand_id), nat.ptr(params), int(bool(train)),
                  int(bool(accumulate)), nat.ptr(ws["partials"]), self._rows, nat.ptr(ind),
                  nat.ptr(x), nat.ptr(w), nat.ptr(f), nat.ptr(ws["flags"]), nat.stream_handle())
@@ -427,14 +428,18 @@ class MonteCarloFlow(ABC):
     # ---------------------------------------------------------------- random numbers
     def generate_random_array(self, n_events, *args):
         """(x, p(x)) for ``n_events`` points (monte_carlo.py:229-247): one
-        sampler launch writing x and w (no bin indices) to HBM."""
-        rnds, xjac_raw, *extra = self._generate_random_array(n_events, *args, want_ind=False)
-        xjac = xjac_raw / (self.xjac * n_events)
-        return rnds, xjac
+        sampler launch writing x and w (no bin indices) to HBM.  The
+        reference's normalisation ``xjac_raw / (xjac n_events)`` is folded into
+        the sampler's weight constant (the Jacobian it is given), so that w is
+        written once, already normalised."""
+        rnds, p, *extra = self._generate_random_array(n_events, *args, want_ind=False,
+                                                      xjac=self.xjac / (self.xjac * n_events))
+        return rnds, p
 
-    def _generate_random_array(self, n_events, *args, want_ind=True):
+    def _generate_random_array(self, n_events, *args, want_ind=True, xjac=None):
         """(x, w[, ind]) of ``n_events`` points, weighted as part of an
-        ``self.n_events`` iteration (monte_carlo.py:249-275)."""
+        ``self.n_events`` iteration (monte_carlo.py:249-275), or with the
+        Jacobian ``xjac`` instead of ``self.xjac``."""
         self._require_gpu()
         n = int(n_events)
         x = torch.empty((n, self.n_dim), dtype=self._rdtype, device=self.device)
@@ -442,7 +447,7 @@ class MonteCarloFlow(ABC):
         ind = torch.empty((n, self.n_dim), dtype=torch.int32, device=self.device) \
             if self._ALG == nat.VF_ALG_VEGAS and want_ind else None
         self._sample(n, 0, self._next_call(), nat.VF_INT_NONE, None, False, False,
-                     u_inj=self._injected(n), ind=ind, x=x, w=w)
+                     u_inj=self._injected(n), ind=ind, x=x, w=w, xjac=xjac)
         if ind is None:
             return x, w
         return x, w, ind

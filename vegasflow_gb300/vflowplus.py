@@ -288,35 +288,44 @@ class VegasFlowPlus(VegasFlow):
                                       f"not {n_events}")
         return self.run_event()
 
-    def _generate_random_array(self, n_events, *args):
-        """(x, w, ind, segm) of one full iteration's layout (vflowplus.py:165-171)."""
+    def _generate_random_array(self, n_events, *args, want_ind=True, xjac=None):
+        """(x, w, ind, segm) of one full iteration's layout (vflowplus.py:165-171);
+        (x, w) alone without ``want_ind``; the weights with the Jacobian
+        ``xjac`` instead of ``self.xjac`` when it is given."""
         self._require_gpu()
         n = self.n_events
         x = torch.empty((n, self.n_dim), dtype=self._rdtype, device=self.device)
         w = torch.empty(n, dtype=self._rdtype, device=self.device)
-        ind = torch.empty((n, self.n_dim), dtype=torch.int32, device=self.device)
+        ind = torch.empty((n, self.n_dim), dtype=torch.int32, device=self.device) if want_ind else None
         xmin, xdelta, xdj = self._limits_ptrs()
         u = self._injected(n)
+        xjac = self.xjac if xjac is None else xjac
         nat.call("vf_plus_sample", self._prec, nat.ptr(self.divisions), self.n_dim, self._n_strat,
-                 self._n_hcubes, nat.ptr(self.n_ev), nat.ptr(self._ev_start), float(self.xjac), xmin,
+                 self._n_hcubes, nat.ptr(self.n_ev), nat.ptr(self._ev_start), float(xjac), xmin,
                  xdelta, float(xdj), nat.ptr(u), self._seed, self._next_call(), nat.VF_INT_NONE, None, 0,
                  None, None, None, max(1, self._rows or self._plus_rows()), nat.ptr(ind), nat.ptr(x),
                  nat.ptr(w), None, nat.stream_handle())
+        if not want_ind:
+            return x, w
         segm = torch.repeat_interleave(torch.arange(self._n_hcubes, device=self.device),
                                        self.n_ev.to(torch.int64))
         return x, w, ind, segm
 
     def generate_random_array(self, n_events, *args):
-        """vflowplus.py:173-185: whole iterations concatenated, cut to ``n_events``."""
+        """vflowplus.py:173-185: whole iterations concatenated, cut to
+        ``n_events``.  The reference's weight normalisation
+        ``w_raw / (xjac n_it) * n_it / n_events`` is folded into the sampler's
+        Jacobian, so each iteration's weights are written once, normalised."""
         rnds, wgts = [], []
         n_it = self.n_events
+        xjac = self.xjac / (self.xjac * n_it) * n_it / n_events
         for _ in range(n_events // n_it + 1):
-            r, w_raw, *_ = self._generate_random_array(n_it)
+            r, w, *_ = self._generate_random_array(n_it, want_ind=False, xjac=xjac)
             rnds.append(r)
-            wgts.append(w_raw / (self.xjac * n_it))
-        final_r = torch.cat(rnds, dim=0)[:n_events]
-        final_w = torch.cat(wgts, dim=0)[:n_events] * n_it / n_events
-        return final_r, final_w
+            wgts.append(w)
+        if len(rnds) == 1:
+            return rnds[0][:n_events], wgts[0][:n_events]
+        return torch.cat(rnds, dim=0)[:n_events], torch.cat(wgts, dim=0)[:n_events]
 
 
 def vegasflowplus_wrapper(integrand, n_dim, n_iter, total_n_events, **kwargs):
