@@ -478,8 +478,10 @@ def main():
         probe_s = pa.elapsed_time(pb) / 1e3
         issue_peak = probe_blocks * 256 * fpt.value / 32 / probe_s  # warp instructions / s
 
-        # end-to-end through the public API with a host-resident grid
-        e2e = e2e_run(inst32, K, dev)
+        # end to end with host buffers: through the C-ABI as a plugin drives it
+        # (the headline), and through the Python API
+        e2e = e2e_abi_run(dev, args.events, K, W, seed=21 + 1000 * rank)
+        e2e_api = e2e_run(inst32, K, dev)
         injected = None if args.no_injected else injected_run(dev, args.events, K, W)
         sampler = None if args.no_injected else sampler_run(dev, args.events, K, W)
         configs = None if args.no_batched else configs_run(dev)
@@ -519,6 +521,7 @@ def main():
                      "peak_source": "measured in this run: vf_issue_probe (independent FFMA chains)",
                      "sampler_ms": 1e3 * samp_mean},
         "e2e": e2e,
+        "e2e_python_api": e2e_api,
         "injected": injected,
         "sampler": sampler,
         "configs": configs,
@@ -785,6 +788,71 @@ def serving_run(seconds):
     m["arrival_window_s"] = seconds
     m["rate_per_s"] = 200.0
     return m
+
+
+def e2e_abi_run(dev, n_events, K, W, seed):
+    """The headline workload end to end through the C-ABI with host buffers, as a
+    plugin binding ``libvegasgb.so`` drives it: the plugin allocates its device
+    buffers once; per step one cudaMemcpyAsync of the grid from pinned host
+    memory, one ``vf_iteration_dev`` call (the fused fp32 sampler and the
+    iteration end: one VegasFlow iteration with float32 refinement), one
+    cudaMemcpyAsync of the refined grid, the (result, sigma) rows and the flags
+    word back into pinned host memory, and one stream synchronize.  Host clock
+    around the K steps (after W untimed ones)."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from vegasflow_gb300 import _native as nat
+
+    lib = nat.load()
+    d, cap = N_DIM, K + W
+    rows = ctypes.c_int(0)
+    nat.check(lib.vf_sample_rows(nat.VF_ALG_VEGAS, nat.VF_PREC_F32, d, nat.VF_INT_SYMGAUSS, 1,
+                                 ctypes.byref(rows)))
+    ng = d * 51
+    nd = ng + 2 * cap + 1  # the grid, the history rows, the flags word (in a float64 slot)
+    dev_buf = torch.zeros(nd, dtype=torch.float64, device=dev)
+    host = torch.zeros(nd, dtype=torch.float64).pin_memory()
+    host[:ng] = torch.linspace(0.0, 1.0, 51, dtype=torch.float64).repeat(d)
+    grid, hist = dev_buf[:ng], dev_buf[ng:ng + 2 * cap]
+    flags = dev_buf[ng + 2 * cap:].view(torch.int32)[:1]
+    partials = torch.empty(rows.value * (2 + 50 * d), dtype=torch.float64, device=dev)
+    avg = torch.zeros(5, dtype=torch.float64, device=dev)
+    counters = torch.zeros(2, dtype=torch.int32, device=dev)
+    params = torch.tensor([A_WIDTH, (1.0 / A_WIDTH / math.sqrt(math.pi)) ** d], dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    sh = nat.stream_handle()
+    torch.cuda.synchronize()
+
+    def step():
+        grid.copy_(host[:ng], non_blocking=True)
+        nat.call("vf_iteration_dev", nat.VF_ALG_VEGAS, nat.VF_PREC_F32, nat.ptr(grid), d, n_events,
+                 1.0 / n_events, None, None, 1.0, seed, nat.ptr(counters[0:1]), nat.ptr(counters[1:2]),
+                 nat.VF_INT_SYMGAUSS, nat.ptr(params), 1, 1.5, nat.ptr(partials), rows.value, nat.ptr(hist),
+                 cap, nat.ptr(avg), nat.ptr(flags), sh)
+        host.copy_(dev_buf, non_blocking=True)
+        stream.synchronize()
+
+    for _ in range(W):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        step()
+    dt = time.perf_counter() - t0
+    res = host[ng:ng + 2 * cap].view(cap, 2).numpy()
+    flag_word = int(host[ng + 2 * cap:].numpy().view(np.int32)[0])
+    exact = math.erf(0.5 / A_WIDTH) ** d
+    last = res[cap - 1]
+    del dev_buf, partials
+    return {"value": n_events * K / dt, "unit": "events/s", "h2d_bytes_per_step": ng * 8,
+            "d2h_bytes_per_step": nd * 8, "ms_per_step": 1e3 * dt / K,
+            "api": "C-ABI: per step cudaMemcpyAsync H2D of the grid (pinned host), vf_iteration_dev, "
+                   "cudaMemcpyAsync D2H of grid + result rows + flags, stream synchronize",
+            "last_iteration": {"result": float(last[0]), "sigma": float(last[1]),
+                               "pull_vs_exact": (float(last[0]) - exact) / float(last[1])},
+            "flags": flag_word}
 
 
 def e2e_run(inst, K, dev):

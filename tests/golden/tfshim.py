@@ -181,15 +181,25 @@ def exp(x):
     return _t(np.exp(np.asarray(x)))
 
 
+def _pair(x, y):
+    """The operands of a binary op: a Python scalar beside a tensor takes the
+    tensor's dtype (converted once, not through float32); two Python scalars
+    follow ``_infer``."""
+    xt, yt = isinstance(x, np.ndarray), isinstance(y, np.ndarray)
+    if xt and not yt:
+        return x, np.asarray(y, dtype=x.dtype)
+    if yt and not xt:
+        return np.asarray(x, dtype=y.dtype), y
+    return _infer(x), _infer(y)
+
+
 def maximum(x, y):
-    return _t(np.fmax(_infer(x), _infer(y)))
+    x, y = _pair(x, y)
+    return _t(np.fmax(x, y))
 
 
 def pow(x, y):  # noqa: A001
-    x = _infer(x)
-    y = _infer(y)
-    if isinstance(y, np.ndarray) and y.ndim == 0 and isinstance(x, np.ndarray):
-        y = y.astype(x.dtype)
+    x, y = _pair(x, y)
     with np.errstate(invalid="ignore"):
         return _t(np.power(x, y))
 
