@@ -4,7 +4,8 @@ import numpy as np
 
 from vegasflow_gb300 import integrands
 from vegasflow_gb300.batch import ITEM_DTYPE, c4_specs
-from vegasflow_gb300.serving import launch_groups, percentile, poisson_workload, request_footprint, step_tables
+from vegasflow_gb300.serving import (SERVE_TILE_MIN, launch_groups, percentile, poisson_workload, request_footprint,
+                                     serving_tile_events, step_tables)
 
 
 def test_step_tables_cover_every_event():
@@ -27,6 +28,30 @@ def test_step_tables_cover_every_event():
     widths = 2 + 50 * np.repeat(n_dim, items["n_tiles"])
     np.testing.assert_array_equal(np.diff(t["tile_row"]), widths[:-1])
     assert t["rows_total"] == widths.sum()
+
+
+def test_served_tile_sizes():
+    """About 512 tiles per request, multiples of 256 events, between 2,048 and
+    65,536 events; tables with one tile size per request cover every event."""
+    n_events = np.array([1, 10_000, 1_000_000, 2_000_000, 10_000_000, 10 ** 9])
+    t = serving_tile_events(n_events)
+    assert np.all(t % 256 == 0) and np.all(t >= SERVE_TILE_MIN) and np.all(t <= 65536)
+    np.testing.assert_array_equal(t, [2048, 2048, 2048, 4096, 19712, 65536])
+    assert np.all((n_events + t - 1) // t <= np.maximum(512, n_events // 65536 + 1))
+    n_dim = [3, 8, 16, 6, 12, 2]
+    tab = step_tables(n_events[:5], n_dim[:5], slots=range(5), stream_ids=range(5), integrand_ids=[1] * 5,
+                      grid_off=range(5), param_off=range(5), tile_events=t[:5])
+    for i, (n, size) in enumerate(zip(n_events[:5], t[:5])):
+        sel = tab["tile_item"] == i
+        assert tab["items"]["n_tiles"][i] == sel.sum() == -(-n // size)
+        assert tab["tile_count"][sel].sum() == n and tab["tile_count"][sel].max() <= size
+        np.testing.assert_array_equal(tab["tile_start"][sel], np.arange(sel.sum()) * size)
+
+
+def test_step_tables_of_no_requests():
+    t = step_tables([], [], [], [], [], [], [], serving_tile_events([]))
+    assert t["n_tiles"] == 0 and t["rows_total"] == 0 and t["items"].size == 0
+    assert t["tile_item"].size == t["tile_row"].size == t["blk_item"].size == 0
 
 
 def test_footprint_grows_with_tiles():

@@ -198,7 +198,8 @@ def test_allocation_failures_fail_only_their_requests():
             raise MemoryError(f"injected {event} failure")
 
     server = VegasServer(max_slots=16, hbm_budget=1e9, seed=7, fault_hook=hook)
-    server.partials = server.partials[:200]  # one request's rows (152) fit, two do not
+    # one request's rows (20,000 events in 10 tiles of 2,048: 10 x 152 doubles) fit, two do not
+    server.partials = server.partials[:2000]
     first = [Request(3, 20_000, integrands.symgauss(0.2), max_iterations=2, rid=i) for i in range(2)]
     for r in first:
         server.submit(r)

@@ -84,22 +84,46 @@ class Request:
         return self.finished - self.arrival
 
 
+# Tile sizes of served requests: a persistent sampler block processes one tile
+# (256 threads), so a request cut into few large tiles runs on few SMs and its
+# iteration takes as long as one block needs for a whole tile (~250 us for 64K
+# events).  A served request is cut into about SERVE_TILES tiles of between
+# SERVE_TILE_MIN and DEFAULT_TILE_EVENTS events (a multiple of 256): small
+# requests spread over the GPU, large ones keep tiles big enough that the
+# per-tile work (histogram clear and flush, the partial row) stays small.  The
+# size depends only on the request's own event count, so its result does not
+# depend on the other requests.
+SERVE_TILES = 512
+SERVE_TILE_MIN = 2048
+
+
+def serving_tile_events(n_events):
+    """Events per tile of a served request of ``n_events`` events (scalar or array)."""
+    n = np.asarray(n_events, dtype=np.int64)
+    t = (n + SERVE_TILES - 1) // SERVE_TILES
+    t = (t + 255) // 256 * 256
+    return np.minimum(DEFAULT_TILE_EVENTS, np.maximum(SERVE_TILE_MIN, t))
+
+
 def step_tables(n_events, n_dim, slots, stream_ids, integrand_ids, grid_off, param_off, tile_events, train=True):
     """The per-step device tables for the active requests (host side, vectorised):
     items, tiles (item, first event, count, partial-row offset) and the
-    iteration-end block table (item, role)."""
+    iteration-end block table (item, role).  ``tile_events``: one tile size for
+    every request, or one per request."""
     n_events = np.asarray(n_events, dtype=np.int64)
     n_dim = np.asarray(n_dim, dtype=np.int64)
     n = n_events.size
+    tile_events = np.broadcast_to(np.asarray(tile_events, dtype=np.int64), n_events.shape)
     n_tiles = (n_events + tile_events - 1) // tile_events
-    tile0 = np.concatenate([[0], np.cumsum(n_tiles)[:-1]]).astype(np.int64)
+    tile0 = np.concatenate([[0], np.cumsum(n_tiles)[:-1]])[:n].astype(np.int64)
     total = int(n_tiles.sum())
     tile_item = np.repeat(np.arange(n, dtype=np.int32), n_tiles)
     k = np.arange(total, dtype=np.int64) - np.repeat(tile0, n_tiles)
-    tile_start = k * tile_events
-    tile_count = np.minimum(tile_events, np.repeat(n_events, n_tiles) - tile_start).astype(np.int32)
+    tile_size = np.repeat(tile_events, n_tiles)
+    tile_start = k * tile_size
+    tile_count = np.minimum(tile_size, np.repeat(n_events, n_tiles) - tile_start).astype(np.int32)
     width = 2 + BINS_MAX * np.repeat(n_dim, n_tiles)
-    tile_row = np.concatenate([[0], np.cumsum(width)[:-1]]).astype(np.int64)
+    tile_row = np.concatenate([[0], np.cumsum(width)[:-1]])[:total].astype(np.int64)
     rows_total = int(width.sum())
     items = np.zeros(n, dtype=ITEM_DTYPE)
     items["n_events"] = n_events
@@ -114,7 +138,7 @@ def step_tables(n_events, n_dim, slots, stream_ids, integrand_ids, grid_off, par
     items["train"] = int(bool(train))
     items["slot"] = slots
     blk_item = np.repeat(np.arange(n, dtype=np.int32), n_dim + 1)
-    starts = np.concatenate([[0], np.cumsum(n_dim + 1)[:-1]])
+    starts = np.concatenate([[0], np.cumsum(n_dim + 1)[:-1]])[:n]
     blk_role = (np.arange(int((n_dim + 1).sum())) - np.repeat(starts, n_dim + 1)).astype(np.int32)
     last = starts + n_dim
     blk_role[last] = -1
@@ -142,9 +166,12 @@ def launch_groups(act, n_tiles, small_blocks):
     return groups
 
 
-def request_footprint(n_dim, n_events, tile_events=DEFAULT_TILE_EVENTS, hist_cap=32):
+def request_footprint(n_dim, n_events, tile_events=None, hist_cap=32):
     """Device bytes a request holds while active: its slot (grid, parameters,
-    history, average, counters) and its partial rows."""
+    history, average, counters) and its partial rows (``tile_events`` None: the
+    served tile size of ``serving_tile_events``)."""
+    if tile_events is None:
+        tile_events = int(serving_tile_events(n_events))
     n_tiles = (n_events + tile_events - 1) // tile_events
     rows = n_tiles * (2 + BINS_MAX * n_dim) * 8
     slot = (MAX_DIM * (BINS_MAX + 1) + PARAMS_PER_SLOT + 2 * hist_cap + 5) * 8 + 8
@@ -167,7 +194,7 @@ class VegasServer:
     control); ``seed`` keys every request's Philox stream (with its request id as
     stream id)."""
 
-    def __init__(self, max_slots=2048, hbm_budget=150e9, tile_events=DEFAULT_TILE_EVENTS, seed=1234,
+    def __init__(self, max_slots=2048, hbm_budget=150e9, tile_events=None, seed=1234,
                  hist_cap=32, device=None, fault_hook=None):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
@@ -176,7 +203,7 @@ class VegasServer:
         preload_kernels(self.device)
         self.max_slots = int(max_slots)
         self.hbm_budget = float(hbm_budget)
-        self.tile_events = int(tile_events)
+        self.tile_events = None if tile_events is None else int(tile_events)  # None: per request
         self.seed = int(seed)
         self.hist_cap = int(hist_cap)
         dev = self.device
@@ -196,6 +223,13 @@ class VegasServer:
             self._blocks[md] = blocks.value
         self.blocks = self._blocks[MAX_DIM]
         self._uniform_row = torch.as_tensor(np.linspace(0.0, 1.0, BINS_MAX + 1), dtype=torch.float64, device=dev)
+        # the active set's device tables and launch arguments (rebuilt when it changes),
+        # their pinned staging buffer, and pinned mirrors for the per-step state read
+        self._prep = None
+        self._tab_host = torch.empty(0, dtype=torch.uint8)
+        self._tab_dev = torch.empty(0, dtype=torch.uint8, device=dev)
+        self._avg_host = torch.empty((self.max_slots, 5), dtype=torch.float64).pin_memory()
+        self._iters_host = torch.empty(self.max_slots, dtype=torch.int32).pin_memory()
         self.free_slots = list(range(self.max_slots - 1, -1, -1))
         self.active = []          # requests on the GPU
         self.waiting = []         # arrived, not admitted yet
@@ -339,62 +373,99 @@ class VegasServer:
         return step_tables([r.n_events for r in act], [r.n_dim for r in act], [r.slot for r in act],
                            [r.rid for r in act], [r.program or r.integrand.integrand_id for r in act],
                            [r.slot * MAX_DIM * (BINS_MAX + 1) for r in act],
-                           [r.slot * PARAMS_PER_SLOT for r in act], self.tile_events)
+                           [r.slot * PARAMS_PER_SLOT for r in act],
+                           self.tile_events if self.tile_events is not None
+                           else serving_tile_events([r.n_events for r in act]))
+
+    _TABLES = ("items", "tile_item", "tile_start", "tile_count", "tile_row", "blk_item", "blk_role")
+
+    def _prepare(self, act, t, stream):
+        """Device tables and launch arguments of the active set ``act`` (tables
+        ``t``): the seven tables packed into one pinned staging buffer and sent
+        with one copy, and every launch's ctypes arguments built once.  Each step
+        ends with a stream synchronize, so the staging and table buffers are idle
+        whenever they are rewritten."""
+        blobs = [t["items"].view(np.uint8)] + [np.ascontiguousarray(t[k]).view(np.uint8) for k in self._TABLES[1:]]
+        offs, total = [], 0
+        for b in blobs:
+            offs.append(total)
+            total += (b.size + 15) // 16 * 16
+        if self._tab_host.numel() < total:
+            cap = max(total, 2 * self._tab_host.numel(), 1 << 16)
+            self._tab_host = torch.empty(cap, dtype=torch.uint8).pin_memory()
+            self._tab_dev = torch.empty(cap, dtype=torch.uint8, device=self.device)
+        h = self._tab_host.numpy()
+        for b, o in zip(blobs, offs):
+            h[o:o + b.size] = b.reshape(-1)
+        self._tab_dev[:total].copy_(self._tab_host[:total], non_blocking=True)
+        base = self._tab_dev.data_ptr()
+        at = {k: base + o for k, o in zip(self._TABLES, offs)}
+        vp = ctypes.c_void_p
+        lib = nat.load()
+        groups = launch_groups(act, t["items"]["n_tiles"], self._blocks[MAX_DIM])
+        if len(groups) > self._queue.numel():
+            self._queue = torch.zeros(2 * len(groups), dtype=torch.int32, device=self.device)
+        launches = []
+        for q, (first, count, md, jit) in enumerate(groups):
+            args = (vp(at["items"]), vp(at["tile_item"] + 4 * first), vp(at["tile_start"] + 8 * first),
+                    vp(at["tile_count"] + 4 * first), vp(at["tile_row"] + 8 * first), count, md,
+                    vp(self._queue.data_ptr() + 4 * q), nat.ptr(self.calls), nat.ptr(self.grids),
+                    nat.ptr(self.params), nat.ptr(self.partials), self.seed, nat.ptr(self._flags),
+                    self._blocks[md], stream)
+            launches.append((lib.vf_batch_sample, args) if jit is None else
+                            (lib.vf_batch_sample_jit, (jit,) + args))
+        launches.append((lib.vf_batch_iteration_end,
+                         (vp(at["items"]), vp(at["blk_item"]), vp(at["blk_role"]), int(t["blk_item"].size),
+                          vp(at["tile_row"]), nat.ptr(self.partials), nat.ptr(self.grids), nat.ptr(self.history),
+                          nat.ptr(self.avg), self.hist_cap, nat.ptr(self.iters), nat.ptr(self.calls),
+                          nat.ptr(self._queue), nat.ptr(self._flags), stream)))
+        slots = np.array([r.slot for r in act], dtype=np.int64)
+        return {"key": self._prep_key(act, stream), "launches": launches, "n_groups": len(groups),
+                "slots": slots, "smax": int(slots.max()) + 1 if slots.size else 0,
+                "events": int(sum(r.n_events for r in act))}
+
+    def _prep_key(self, act, stream):
+        return (tuple(r.rid for r in act), stream.value, self.partials.data_ptr(), self._queue.data_ptr())
 
     def step(self, now_fn):
         """Advance every active request by one iteration, then retire finished ones."""
         # ordered by (program, dimension class): each run of tiles goes to one
         # sampler launch (n_dim <= 8: the class with smaller shared tables)
         act = sorted(self.active, key=lambda r: (r.program, r.n_dim > 8))
-        t = self._tables(act)
-        if t["rows_total"] > self.partials.numel():
-            try:
-                self._fault("grow", rows=t["rows_total"])
-                self.partials = torch.zeros(int(t["rows_total"] * 1.5), dtype=torch.float64, device=self.device)
-            except (RuntimeError, MemoryError) as exc:
-                # no room for this step's partial rows: fail the newest requests until the
-                # rest fit the buffer there is, and take the step with those
-                now = now_fn()
-                while act and t["rows_total"] > self.partials.numel():
-                    self._finish(act.pop(), "failed", now, f"device allocation failed: {exc}")
-                    t = self._tables(act)
-                self.active = act
-                if not act:
-                    return
-        dev = self.device
-        items = torch.from_numpy(t["items"].view(np.uint8)).to(dev, non_blocking=True)
-        arrs = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev, non_blocking=True)
-                for k in ("tile_item", "tile_start", "tile_count", "tile_row", "blk_item", "blk_role")}
-        lib = nat.load()
-        s = nat.stream_handle()
-        groups = launch_groups(act, t["items"]["n_tiles"], self._blocks[MAX_DIM])
-        if len(groups) > self._queue.numel():
-            self._queue = torch.zeros(2 * len(groups), dtype=torch.int32, device=dev)
-        for q, (first, count, md, jit) in enumerate(groups):
-            args = (nat.ptr(items), nat.ptr(arrs["tile_item"][first:]), nat.ptr(arrs["tile_start"][first:]),
-                    nat.ptr(arrs["tile_count"][first:]), nat.ptr(arrs["tile_row"][first:]), count, md,
-                    nat.ptr(self._queue[q:q + 1]), nat.ptr(self.calls), nat.ptr(self.grids), nat.ptr(self.params),
-                    nat.ptr(self.partials), self.seed, nat.ptr(self._flags), self._blocks[md], s)
-            if jit is None:
-                nat.check(lib.vf_batch_sample(*args))
-            else:
-                nat.check(lib.vf_batch_sample_jit(jit, *args))
-        nat.check(lib.vf_batch_iteration_end(nat.ptr(items), nat.ptr(arrs["blk_item"]), nat.ptr(arrs["blk_role"]),
-                                             int(t["blk_item"].size), nat.ptr(arrs["tile_row"]),
-                                             nat.ptr(self.partials), nat.ptr(self.grids), nat.ptr(self.history),
-                                             nat.ptr(self.avg), self.hist_cap, nat.ptr(self.iters),
-                                             nat.ptr(self.calls), nat.ptr(self._queue), nat.ptr(self._flags), s))
-        if len(groups) > 1:
-            self._queue[1:len(groups)].zero_()  # the other launches' counters (the iteration end re-arms the first)
-        slots = torch.as_tensor([r.slot for r in act], dtype=torch.int64, device=dev)
-        state = torch.cat([self.avg[slots][:, 2:4].reshape(-1),
-                           self.iters[slots].to(torch.float64)]).cpu().numpy()
+        stream = nat.stream_handle()
+        prep = self._prep
+        if prep is None or prep["key"] != self._prep_key(act, stream):
+            t = self._tables(act)
+            if t["rows_total"] > self.partials.numel():
+                try:
+                    self._fault("grow", rows=t["rows_total"])
+                    self.partials = torch.zeros(int(t["rows_total"] * 1.5), dtype=torch.float64, device=self.device)
+                except (RuntimeError, MemoryError) as exc:
+                    # no room for this step's partial rows: fail the newest requests until the
+                    # rest fit the buffer there is, and take the step with those
+                    now = now_fn()
+                    while act and t["rows_total"] > self.partials.numel():
+                        self._finish(act.pop(), "failed", now, f"device allocation failed: {exc}")
+                        t = self._tables(act)
+                    self.active = act
+                    if not act:
+                        return
+            prep = self._prep = self._prepare(act, t, stream)
+        for fn, args in prep["launches"]:
+            nat.check(fn(*args))
+        if prep["n_groups"] > 1:
+            self._queue[1:prep["n_groups"]].zero_()  # the other launches' counters (the iteration end re-arms the first)
+        # the state of the slots in use: two copies into pinned memory, one synchronize
+        smax = prep["smax"]
+        self._avg_host[:smax].copy_(self.avg[:smax], non_blocking=True)
+        self._iters_host[:smax].copy_(self.iters[:smax], non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
         now = now_fn()
-        n = len(act)
-        means = state[: 2 * n: 2]
-        sigmas = state[1: 2 * n: 2]
-        its = state[2 * n:].astype(np.int64)
-        self.events_done += int(sum(r.n_events for r in act))
+        sl = prep["slots"]
+        avg = self._avg_host.numpy()
+        means, sigmas = avg[sl, 2], avg[sl, 3]
+        its = self._iters_host.numpy()[sl].astype(np.int64)
+        self.events_done += prep["events"]
         self.steps += 1
         still = []
         for r, m, sg, it in zip(act, means, sigmas, its):
