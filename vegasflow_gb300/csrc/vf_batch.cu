@@ -157,7 +157,7 @@ int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, cons
   a.flags = flags;
   a.alpha = 1.5;
   a.hist_cap = hist_cap;
-  vf::vf_batch_end_kernel<<<n_blocks, 256, 0, (cudaStream_t)stream>>>(a);
+  vf::vf_batch_end_kernel<<<n_blocks, VF_BATCH_END_THREADS, 0, (cudaStream_t)stream>>>(a);
   return launched("vf_batch_iteration_end");
 }
 
