@@ -273,11 +273,15 @@ int vf_batch_sample_jit(int integrand_id, const vf_batch_item* items, const int*
 /* Per integral: sums of its tile rows in tile order, sigma, history[slot][iters[slot]],
  * the weighted average avg[slot][5], then iters[slot] += 1, calls[slot] += 1; per
  * (integral, dimension) block: refinement of that grid row; *queue = 0.  Block b serves
- * integral blk_item[b] in role blk_role[b] (a dimension, or -1 for the sums). */
+ * integral blk_item[b] in role blk_role[b] (a dimension, or -1 for the sums).
+ * status: nullable [items][3] doubles receiving, for item i, the running mean,
+ * its sigma and the iterations in the average after this one (avg[slot][2],
+ * avg[slot][3], iters[slot]); device memory, or pinned host memory that the
+ * device can address (read it after the stream synchronizes: no copy needed). */
 int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, const int* blk_role, int n_blocks,
                            const long long* tile_row, const double* partials, double* grids, double* history,
                            double* avg, int hist_cap, int* iters, unsigned int* calls, int* queue, int* flags,
-                           void* stream);
+                           double* status, void* stream);
 
 /* VegasFlow.refine_grid(arr_res2) (vflow.py:349-362): hist [n_dim][50]. */
 int vf_refine_grid(double* grid, const double* hist, int n_dim, double alpha, int* flags,

@@ -83,7 +83,7 @@ SIGNATURES = {
     "vf_batch_blocks": [_I, _P, _P],
     "vf_batch_sample": [_P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],
     "vf_batch_sample_jit": [_I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _U64, _P, _I, _P],
-    "vf_batch_iteration_end": [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P],
+    "vf_batch_iteration_end": [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P, _P],
     "vf_jit_integrand": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, _P],
     "vf_jit_check": [ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, ctypes.c_char_p, _I],
     "vf_preload": [],

@@ -178,7 +178,7 @@ class VegasBatch:
                                              nat.ptr(self._tile_row), nat.ptr(self.partials),
                                              nat.ptr(self.grids), nat.ptr(self.history), nat.ptr(self.avg),
                                              self.hist_cap, nat.ptr(self._iters), nat.ptr(self._calls),
-                                             nat.ptr(self._queue), nat.ptr(self._flags), s))
+                                             nat.ptr(self._queue), nat.ptr(self._flags), None, s))
         if len(self._groups) > 1:
             self._queue[1:].zero_()  # the iteration end re-arms the first counter
 

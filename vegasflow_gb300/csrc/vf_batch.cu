@@ -24,6 +24,19 @@ int launched(const char* what) {
   return VF_OK;
 }
 
+// The device address of `p`: `p` itself for device memory, the mapped address
+// for pinned host memory (the same pointer under unified addressing).
+bool device_address(double* p, double** out) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.devicePointer == nullptr ||
+      (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeHost && at.type != cudaMemoryTypeManaged)) {
+    cudaGetLastError();  // clear the lookup's error
+    return false;
+  }
+  *out = static_cast<double*>(at.devicePointer);
+  return true;
+}
+
 // The sampler of a dimension class (n_dim <= 8, or any).
 const void* sample_kernel_for(int max_dim) {
   return max_dim <= 8 ? (const void*)vf::vf_batch_sample_kernel<8> : (const void*)vf::vf_batch_sample_kernel<16>;
@@ -137,11 +150,15 @@ int vf_batch_sample_jit(int integrand_id, const vf_batch_item* items, const int*
 int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, const int* blk_role, int n_blocks,
                            const long long* tile_row, const double* partials, double* grids, double* history,
                            double* avg, int hist_cap, int* iters, unsigned int* calls, int* queue, int* flags,
-                           void* stream) {
+                           double* status, void* stream) {
   if (!items || !blk_item || !blk_role || !tile_row || !partials || !grids || !history || !avg || !iters ||
       !calls || !queue ||
       n_blocks < 1 || hist_cap < 1)
     return err(VF_ERR_ARG, "vf_batch_iteration_end: NULL buffer or bad sizes");
+  double* status_dev = nullptr;
+  if (status && !device_address(status, &status_dev))
+    return err(VF_ERR_ARG, "vf_batch_iteration_end: status is neither device memory nor host memory the device "
+                           "can address");
   vf::BatchEndArgs a;
   a.items = reinterpret_cast<const vf::BatchItem*>(items);
   a.blk_item = blk_item;
@@ -155,6 +172,7 @@ int vf_batch_iteration_end(const vf_batch_item* items, const int* blk_item, cons
   a.calls = calls;
   a.queue = queue;
   a.flags = flags;
+  a.status = status_dev;
   a.alpha = 1.5;
   a.hist_cap = hist_cap;
   vf::vf_batch_end_kernel<<<n_blocks, VF_BATCH_END_THREADS, 0, (cudaStream_t)stream>>>(a);

@@ -25,6 +25,7 @@ struct BatchEndArgs {
   unsigned int* calls;      // [slots] Philox call counters
   int* queue;               // the sampler's work counter, re-armed here
   int* flags;
+  double* status;           // nullable [items][3]: mean, sigma, iterations (device address)
   double alpha;
   int hist_cap;
 };
@@ -104,6 +105,12 @@ __global__ void __launch_bounds__(VF_BATCH_END_THREADS) vf_batch_end_kernel(cons
     if (!isfinite(res) && a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
     a.iters[slot] = iter + 1;
     a.calls[slot] += 1u;
+    if (a.status) {
+      double* st = a.status + 3LL * item;
+      st[0] = mean;
+      st[1] = av[3];
+      st[2] = (double)(iter + 1);
+    }
   }
   __syncthreads();
   const double chi2 = block_chi2(a.history + (long long)slot * a.hist_cap * 2, 2, 1, s_hs + 1, s_mean);

@@ -228,8 +228,9 @@ class VegasServer:
         self._prep = None
         self._tab_host = torch.empty(0, dtype=torch.uint8)
         self._tab_dev = torch.empty(0, dtype=torch.uint8, device=dev)
-        self._avg_host = torch.empty((self.max_slots, 5), dtype=torch.float64).pin_memory()
-        self._iters_host = torch.empty(self.max_slots, dtype=torch.int32).pin_memory()
+        # per step, the iteration end writes each active request's (mean, sigma,
+        # iterations) here, in pinned host memory the device addresses directly
+        self._status = torch.zeros((self.max_slots, 3), dtype=torch.float64).pin_memory()
         self.free_slots = list(range(self.max_slots - 1, -1, -1))
         self.active = []          # requests on the GPU
         self.waiting = []         # arrived, not admitted yet
@@ -418,10 +419,8 @@ class VegasServer:
                          (vp(at["items"]), vp(at["blk_item"]), vp(at["blk_role"]), int(t["blk_item"].size),
                           vp(at["tile_row"]), nat.ptr(self.partials), nat.ptr(self.grids), nat.ptr(self.history),
                           nat.ptr(self.avg), self.hist_cap, nat.ptr(self.iters), nat.ptr(self.calls),
-                          nat.ptr(self._queue), nat.ptr(self._flags), stream)))
-        slots = np.array([r.slot for r in act], dtype=np.int64)
+                          nat.ptr(self._queue), nat.ptr(self._flags), vp(self._status.data_ptr()), stream)))
         return {"key": self._prep_key(act, stream), "launches": launches, "n_groups": len(groups),
-                "slots": slots, "smax": int(slots.max()) + 1 if slots.size else 0,
                 "events": int(sum(r.n_events for r in act))}
 
     def _prep_key(self, act, stream):
@@ -455,28 +454,32 @@ class VegasServer:
             nat.check(fn(*args))
         if prep["n_groups"] > 1:
             self._queue[1:prep["n_groups"]].zero_()  # the other launches' counters (the iteration end re-arms the first)
-        # the state of the slots in use: two copies into pinned memory, one synchronize
-        smax = prep["smax"]
-        self._avg_host[:smax].copy_(self.avg[:smax], non_blocking=True)
-        self._iters_host[:smax].copy_(self.iters[:smax], non_blocking=True)
+        # the iteration end has written every active request's state into pinned
+        # host memory: one synchronize, no copy
         torch.cuda.current_stream(self.device).synchronize()
         now = now_fn()
-        sl = prep["slots"]
-        avg = self._avg_host.numpy()
-        means, sigmas = avg[sl, 2], avg[sl, 3]
-        its = self._iters_host.numpy()[sl].astype(np.int64)
+        n = len(act)
+        st = self._status.numpy()[:n]
+        means, sigmas, its = st[:, 0], st[:, 1], st[:, 2].astype(np.int64)
+        target = np.array([r.target_rel_sigma for r in act]) if n > 1 else act[0].target_rel_sigma
+        cap = np.array([r.max_iterations for r in act]) if n > 1 else act[0].max_iterations
+        with np.errstate(invalid="ignore", divide="ignore"):
+            conv = np.isfinite(means) & np.isfinite(sigmas) & (means != 0.0) & (sigmas / np.abs(means) <= target)
+        done = conv | (its >= cap)
         self.events_done += prep["events"]
         self.steps += 1
-        still = []
-        for r, m, sg, it in zip(act, means, sigmas, its):
-            r.iterations = int(it)
-            r.result, r.sigma = float(m), float(sg)
-            conv = math.isfinite(m) and math.isfinite(sg) and m != 0.0 and sg / abs(m) <= r.target_rel_sigma
-            if conv or it >= r.max_iterations:
-                self._finish(r, "converged" if conv else "finished", now)
-            else:
-                still.append(r)
-        self.active = still
+        for r, m, sg, it in zip(act, means.tolist(), sigmas.tolist(), its.tolist()):
+            r.iterations, r.result, r.sigma = it, m, sg
+        if done.any():
+            still = []
+            for r, c, d in zip(act, conv.tolist(), done.tolist()):
+                if d:
+                    self._finish(r, "converged" if c else "finished", now)
+                else:
+                    still.append(r)
+            self.active = still
+        else:
+            self.active = act
 
     # ---------------------------------------------------------------- the loop
     def run(self, requests, realtime=True, time_limit=None):
