@@ -138,6 +138,29 @@ def _drive(server, steps, now=0.0):
             server.step(lambda: now)
 
 
+def test_status_rows_are_the_slot_state():
+    """The iteration end writes each active request's (mean, sigma, iterations)
+    into the server's pinned status array, in the order of the step's items:
+    after every step they equal the slots' device state, and requests joining
+    and leaving reorder the items."""
+    server = VegasServer(max_slots=32, hbm_budget=1e9, seed=5)
+    reqs = [Request(d, n, integrands.symgauss(0.2), target_rel_sigma=1e-12, max_iterations=50, rid=i)
+            for i, (d, n) in enumerate([(3, 20_000), (9, 200_000), (5, 1_000_000), (12, 50_000)])]
+    for r in reqs[:3]:
+        server.submit(r)
+    for k in range(4):
+        if k == 2:
+            server.submit(reqs[3])
+            server.cancel(reqs[1].rid)
+        _drive(server, 1)
+        avg = server.avg.cpu().numpy()
+        iters = server.iters.cpu().numpy()
+        for r in server.active:
+            assert r.result == avg[r.slot, 2] and r.sigma == avg[r.slot, 3]
+            assert r.iterations == iters[r.slot]
+    assert reqs[1].status == "cancelled" and reqs[3].iterations == 2
+
+
 def test_rejections_do_not_stop_the_server():
     server = VegasServer(max_slots=64, hbm_budget=2e7, seed=3)
     good = Request(3, 50_000, integrands.symgauss(0.2), target_rel_sigma=1e-9, max_iterations=3, rid=0)
