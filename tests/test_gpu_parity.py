@@ -272,14 +272,21 @@ def test_abi_rejects_bad_arguments():
     assert rc == nat.VF_ERR_UNSUPPORTED
 
 
-@pytest.mark.parametrize("spread", [1.0, 4.0])
-def test_float32_refinement_close_to_float64(spread):
-    """vf_iteration_end with train=2 (the fp32 form's float32 refinement) moves
-    the edges to within float32 rounding of the float64 refinement (train=1),
-    keeps them ordered, and keeps the end points."""
-    rng = np.random.default_rng(int(spread))
+@pytest.mark.parametrize("spread,empty,scale", [(1.0, 0.0, 1e-3), (4.0, 0.0, 1e-3), (8.0, 0.0, 1e-3),
+                                                (2.0, 0.7, 1e-3), (2.0, 0.95, 1e-3), (2.0, 0.8, 1e12),
+                                                (2.0, 0.8, 1e-40), (1.0, 1.0, 1.0)])
+def test_float32_refinement_close_to_float64(spread, empty, scale):
+    """vf_iteration_end with train=2 (the fp32 form's float32 refinement, its
+    rebinning walk evaluated in parallel in closed form) moves the edges to
+    within float32 rounding of the float64 refinement (train=1, the reference's
+    sequential walk), keeps them ordered, and keeps the end points -- also for
+    histograms spread over many decades, with most (or all) bins empty, and at
+    scales where the reference's 1e-30 floor leaves float32's range once the
+    histogram is scaled to a largest bin of 1."""
+    rng = np.random.default_rng(int(spread) + int(10 * empty))
     n_dim = 6
-    hist = np.exp(spread * rng.standard_normal((n_dim, 50))) * 1e-3
+    hist = np.exp(spread * rng.standard_normal((n_dim, 50))) * scale
+    hist[rng.random((n_dim, 50)) < empty] = 0.0
     row = np.concatenate([[1.0, 1.0], hist.reshape(-1)])
     grid = np.sort(rng.random((n_dim, 51)), axis=1)
     grid[:, 0], grid[:, -1] = 0.0, 1.0

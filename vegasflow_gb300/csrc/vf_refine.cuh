@@ -167,12 +167,24 @@ __device__ inline void refine_dimension(const double* h, double* row, double alp
 
 // The same refinement in float32 arithmetic -- the reference's float32 mode
 // (configflow.py float switch) -- for the fp32 sampler's grids: the float64
-// histogram is scaled by a power of two so its largest bin is about 1 (the
-// refinement depends only on ratios, apart from the 1e-30 floor, which then
-// applies relative to the largest bin), the smoothing, logarithms, damping and
-// the rebinning walk run in float32 (a few hundred cycles instead of the
-// float64 pipe's ~15,000 on this part), and the new edges are made
-// non-decreasing before they are stored as float64.
+// histogram is scaled by a power of two 2^-e so its largest bin is about 1 (the
+// refinement depends only on ratios and differences of logarithms), and the
+// smoothed values are floored at the reference's absolute 1e-30 (vflow.py:159),
+// i.e. at 1e-30 2^-e in scaled units, with the floor's logarithm carried
+// separately (the scaled floor itself can leave float32's range: empty bins of
+// a histogram whose largest bin is above ~1e8 would otherwise get a weight of
+// 0, and flooring the scaled values at 1e-30 moved the edges of sparse
+// histograms by up to 0.1), the smoothing, logarithms, damping and
+// the rebinning run in float32 (a few hundred cycles instead of the float64
+// pipe's ~15,000 on this part), and the new edges are made non-decreasing
+// before they are stored as float64.  The rebinning walk of vflow.py:178-205
+// (advance while the carried weight is below ave, subtract ave per new edge)
+// is evaluated in parallel in its closed form: with P(i) the prefix sums of the
+// weights, new edge k + 1 lies in the first bin n with P(n) >= (k + 1) ave, at
+// the fraction (P(n) - (k + 1) ave) / wei[n] from its upper end -- a warp scan
+// and one binary search per edge instead of one thread's ~100 dependent steps
+// (which took ~4 us); the ordering of the edges is a prefix maximum.  The
+// roundings differ from the sequential walk's by a few float32 ulps.
 __device__ inline float sum50_pairwise_f(const float* v) {
   const int j = threadIdx.x & 31;
   float r = 0.0f;
@@ -196,8 +208,10 @@ __device__ inline void refine_dimension_f32(const double* h, double* row, double
   __shared__ float edge[VF_EDGES];
   __shared__ float sum_t;
   __shared__ int emax;
-  __shared__ int walk_bin[VF_BINS - 1];
-  __shared__ float walk_weight[VF_BINS - 1];
+  __shared__ float prefix[VF_BINS];
+  __shared__ float ave_sh;
+  __shared__ float lsm[VF_BINS];        // log of the floored smoothed values (scaled)
+  __shared__ float floor_sh, lfloor_sh;  // the floor 1e-30 in scaled units and its logarithm
   const int t = threadIdx.x;
   if (t < VF_EDGES) sub[t] = (float)row[t];
   if (t < 32) {  // the largest binary exponent among the 50 bins (integer max over the bit patterns)
@@ -207,7 +221,21 @@ __device__ inline void refine_dimension_f32(const double* h, double* row, double
       e = ex > e ? ex : e;
     }
     e = __reduce_max_sync(0xffffffffu, e);
-    if (t == 0) emax = e > 1000 ? 1000 : e;
+    if (t == 0) {
+      const int em = e > 1000 ? 1000 : e;
+      emax = em;
+      // 1e-30 2^-em: 0 or denormal when the histogram is large (only its
+      // logarithm matters then), capped at 1e30 when it is tiny (every bin is
+      // floored then, and the weights are uniform whatever the common value)
+      float fl = ldexpf(1e-30f, -em);
+      float lfl = -69.07755279f - (float)em * 0.69314718f;
+      if (!(fl <= 1e30f)) {
+        fl = 1e30f;
+        lfl = 69.07755279f;
+      }
+      floor_sh = fl;
+      lfloor_sh = lfl;
+    }
   }
   __syncthreads();
   if (t < VF_BINS) hf[t] = (float)(h[t] * __longlong_as_double((long long)(1023 - emax) << 52));  // h 2^-emax
@@ -217,7 +245,10 @@ __device__ inline void refine_dimension_f32(const double* h, double* row, double
     const float right = t < VF_BINS - 1 ? hf[t + 1] : 0.0f;
     const float v = (hf[t] + right) + left;
     const float meaner = (t == 0 || t == VF_BINS - 1) ? 2.0f : 3.0f;
-    sm[t] = fmaxf(v / meaner, 1e-30f);
+    const float q = v / meaner;
+    const bool floored = q < floor_sh || q == 0.0f;
+    sm[t] = floored ? floor_sh : q;
+    lsm[t] = floored ? lfloor_sh : logf(q);
   }
   __syncthreads();
   if (t < 32) {
@@ -226,50 +257,71 @@ __device__ inline void refine_dimension_f32(const double* h, double* row, double
   }
   __syncthreads();
   if (t < VF_BINS) {
-    const float aux = (1.0f - sm[t] / sum_t) / (logf(sum_t) - logf(sm[t]));
+    const float aux = (1.0f - sm[t] / sum_t) / (logf(sum_t) - lsm[t]);
     wei[t] = alpha == 1.5 ? aux * sqrtf(aux) : powf(aux, (float)alpha);
   }
   __syncthreads();
   if (t < 32) {
     const float total = sum50_pairwise_f(wei);
-    if (t == 0) {
-      const float ave = total / VF_BINS;
-      float bin_weight = 0.0f;
-      int n_bin = -1;
-      int overrun = 0;
-      for (int k = 0; k < VF_BINS - 1; ++k) {
-        while (bin_weight < ave) {
-          if (n_bin + 1 >= VF_BINS) {
-            overrun = 1;
-            break;
-          }
-          n_bin += 1;
-          bin_weight += wei[n_bin];
-        }
-        bin_weight -= ave;
-        walk_bin[k] = n_bin;
-        walk_weight[k] = bin_weight;
-      }
-      if (overrun && flags) atomicOr(flags, VF_FLAG_REFINE_OVERRUN);
+    // inclusive prefix sums P(i) of the weights: two bins per lane, a warp scan
+    const int i0 = 2 * t, i1 = 2 * t + 1;
+    const float a0 = i0 < VF_BINS ? wei[i0] : 0.0f;
+    const float a1 = i1 < VF_BINS ? wei[i1] : 0.0f;
+    float sc = a0 + a1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float u = __shfl_up_sync(0xffffffffu, sc, o);
+      if (t >= o) sc += u;
     }
+    float ex = __shfl_up_sync(0xffffffffu, sc, 1);
+    if (t == 0) ex = 0.0f;
+    const float p0 = ex + a0;
+    if (i0 < VF_BINS) prefix[i0] = p0;
+    if (i1 < VF_BINS) prefix[i1] = p0 + a1;
+    if (t == 0) ave_sh = total / VF_BINS;
   }
   __syncthreads();
   if (t < VF_BINS - 1) {
-    const int n_bin = walk_bin[t];
-    const float cur = n_bin >= 0 ? sub[n_bin + 1] : 0.0f;
-    const float prev = n_bin >= 1 ? sub[n_bin] : 0.0f;
-    const float w = wei[n_bin >= 0 ? n_bin : VF_BINS - 1];
-    edge[t + 1] = cur - (cur - prev) * walk_weight[t] / w;
+    // new edge t + 1: the first bin whose prefix reaches (t + 1) ave
+    const float target = (float)(t + 1) * ave_sh;
+    int lo = 0, hi = VF_BINS;  // P(lo - 1) < target <= P(hi), as far as known
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (prefix[mid] < target)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    int n_bin = lo;
+    if (n_bin >= VF_BINS) {  // the walk would run past the last bin (rounding): the reference indexes out of range
+      n_bin = VF_BINS - 1;
+      if (flags) atomicOr(flags, VF_FLAG_REFINE_OVERRUN);
+    }
+    const float carried = prefix[n_bin] - target;
+    const float cur = sub[n_bin + 1];
+    const float prev = n_bin >= 1 ? sub[n_bin] : 0.0f;  // the walk starts from prev = 0 (vflow.py:197-199)
+    edge[t + 1] = cur - (cur - prev) * carried / wei[n_bin];
   }
   __syncthreads();
-  if (t == 0) {  // float32 rounding can swap two edges a few ulps apart: keep them ordered
-    float lo = 0.0f;
-    row[0] = 0.0;
-    for (int k = 1; k < VF_BINS; ++k) {
-      lo = fmaxf(lo, fminf(edge[k], 1.0f));
-      row[k] = (double)lo;
+  if (t < 32) {  // float32 rounding can swap two edges a few ulps apart: keep them ordered (a prefix maximum)
+    const int k0 = 2 * t + 1, k1 = 2 * t + 2;  // edges 1..49
+    const float e0 = k0 < VF_BINS ? fminf(edge[k0], 1.0f) : 0.0f;
+    const float e1 = k1 < VF_BINS ? fminf(edge[k1], 1.0f) : 0.0f;
+    float m = fmaxf(e0, e1);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float u = __shfl_up_sync(0xffffffffu, m, o);
+      if (t >= o) m = fmaxf(m, u);
     }
-    row[VF_BINS] = 1.0;
+    float before = __shfl_up_sync(0xffffffffu, m, 1);
+    if (t == 0) before = 0.0f;
+    const float m0 = fmaxf(before, e0);
+    if (k0 < VF_BINS) row[k0] = (double)m0;
+    if (k1 < VF_BINS) row[k1] = (double)fmaxf(m0, e1);
+    if (t == 0) {
+      row[0] = 0.0;
+      row[VF_BINS] = 1.0;
+    }
   }
   __syncthreads();
 }
