@@ -84,7 +84,7 @@ vf_iteration_end_kernel(const IterEndArgs a) {
   }
   // ---- the sums, one output at a time
   __shared__ double red[2][VF_END_THREADS / 32];
-  __shared__ double mean_sh;
+  __shared__ double mean_sh, sums_sh[2];
   const int lane = t & 31, warp = t >> 5;
   for (int j = 0; j < K; ++j) {
     double s1 = 0.0, s2 = 0.0;
@@ -125,13 +125,20 @@ vf_iteration_end_kernel(const IterEndArgs a) {
       // history row 0 starts a new average: the buffer's previous contents are not read
       av[0] = it == 0 ? __dmul_rn(res, wgt) : __dadd_rn(av[0], __dmul_rn(res, wgt));
       av[1] = it == 0 ? wgt : __dadd_rn(av[1], wgt);
-      const double mean = av[0] / av[1];
-      av[2] = mean;
-      av[3] = sqrt(1.0 / av[1]);
-      mean_sh = mean;
+      sums_sh[0] = av[0];
+      sums_sh[1] = av[1];
       if (!isfinite(res) || !isfinite(res2)) {
         if (a.flags) atomicOr(a.flags, VF_FLAG_NONFINITE);
       }
+    }
+    __syncthreads();
+    // the mean and its sigma, two independent float64 chains on two warps
+    if (t == 0) {
+      const double mean = sums_sh[0] / sums_sh[1];
+      a.avg[5 * j + 2] = mean;
+      mean_sh = mean;
+    } else if (t == 32) {
+      a.avg[5 * j + 3] = sqrt(1.0 / sums_sh[1]);
     }
     __syncthreads();
     const double chi2 = block_chi2(a.history + j, 2 * K, K, it + 1, mean_sh);

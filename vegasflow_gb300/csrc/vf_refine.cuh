@@ -46,6 +46,18 @@ __device__ inline void sum_hist_columns(RowAt row_at, int rows, double* hsm, dou
 // cycles on this part: one thread walking a long history was the iteration
 // end's slowest step.)
 __device__ inline double block_chi2(const double* rows, long long stride, int sig_off, int count, double mean) {
+  if (count <= 32) {  // one warp holds every row (the other warps would add zeros): no block pass
+    double c = 0.0;
+    if (threadIdx.x < 32) {
+      if ((int)threadIdx.x < count) {
+        const double r = rows[(long long)threadIdx.x * stride], sg = rows[(long long)threadIdx.x * stride + sig_off];
+        c = (r - mean) * (r - mean) / (sg * sg);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    return c;
+  }
   __shared__ double part[32];
   double c = 0.0;
   for (int i = threadIdx.x; i < count; i += blockDim.x) {
