@@ -66,6 +66,23 @@ def test_vegas_graph_matches_eager(precision):
     assert abs(r_g[0] - 1.0) < 5 * r_g[1]
 
 
+def test_unrolled_graph_matches_eager():
+    """11 iterations: one replay of an 8-iteration graph, then three replays of
+    the one-iteration graph; the same history as eager launches."""
+    from vegasflow_gb300.monte_carlo import GRAPH_UNROLL
+    assert GRAPH_UNROLL == 8
+    eager, graph = _pair(VegasFlow, "fp64", integrands.symgauss())
+    r_e = eager.run_integration(11)
+    r_g = graph.run_integration(11)
+    np.testing.assert_allclose(r_g, r_e, rtol=1e-10)
+    assert sorted(graph._graphs_unrolled) == [8]
+    hist_e = np.array([h[:2] for h in eager._history], dtype=float)
+    hist_g = np.array([h[:2] for h in graph._history], dtype=float)
+    assert hist_g.shape == (11, 2)
+    np.testing.assert_allclose(hist_g, hist_e, rtol=1e-10)
+    np.testing.assert_allclose(graph.divisions.cpu().numpy(), eager.divisions.cpu().numpy(), rtol=0, atol=1e-12)
+
+
 def test_graph_reused_and_recaptured_on_freeze():
     eager, graph = _pair(VegasFlow, "fp32", integrands.symgauss())
     eager.run_integration(3)

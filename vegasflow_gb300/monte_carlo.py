@@ -54,6 +54,12 @@ from .integrands import DeviceIntegrand
 
 logger = logging.getLogger("vegasflow.monte_carlo")
 
+# Iterations captured in one CUDA graph at most (cuda_graph=True, run_integration
+# without per-iteration logging): one graph launch and one host call per
+# GRAPH_UNROLL iterations.  Measured on the 4-D Gaussian at 1e6 events: a replay
+# of one iteration costs ~6 us of host time and the graph launches add gaps.
+GRAPH_UNROLL = 8
+
 
 class _nvtx:
     """An NVTX range (for Nsight timelines) around a block of host calls when
@@ -157,6 +163,7 @@ class MonteCarloFlow(ABC):
         self._differentiable = False
         self._graph = None
         self._graph_key = None
+        self._graphs_unrolled = {}
 
         if xmin is not None or xmax is not None:  # monte_carlo.py:159-175
             if xmin is None or xmax is None:
@@ -610,9 +617,26 @@ class MonteCarloFlow(ABC):
                 ws["history"].data_ptr(), ws["history"].shape[0], ws["avg"].data_ptr(), ws["flags"].data_ptr(),
                 ws["counters"].data_ptr(), addr(xmin), addr(xdelta), xdj, self._shape)
 
-    def _graph_for(self, n_iter):
-        """The CUDA graph of one iteration (captured again whenever an argument
-        of the captured call changed), with room for ``n_iter`` history rows."""
+    def _capture(self, ws, unroll):
+        """A CUDA graph of ``unroll`` consecutive iteration calls."""
+        from .utils import capture_guard, preload_kernels
+        preload_kernels(self.device)
+        torch.cuda.synchronize(self.device)
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        with capture_guard(), torch.cuda.stream(side):
+            with torch.cuda.graph(g, stream=side):
+                for _ in range(unroll):
+                    self._graph_call(ws)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        return g
+
+    def _graph_for(self, n_iter, unroll=1):
+        """The CUDA graph of ``unroll`` iterations (captured again whenever an
+        argument of the captured call changed), with room for ``n_iter``
+        history rows.  ``self._graph`` is the one-iteration graph; graphs of
+        several iterations are kept beside it for the same arguments."""
         ws = self._workspace()
         if ws["history"].shape[0] < n_iter:
             self._state_rows(ws, max(n_iter, 2 * ws["history"].shape[0]))
@@ -621,37 +645,43 @@ class MonteCarloFlow(ABC):
         self._apply_shape()
         key = self._graph_signature(ws)
         if self._graph is None or self._graph_key != key:
-            from .utils import capture_guard, preload_kernels
-            preload_kernels(self.device)
-            torch.cuda.synchronize(self.device)
-            side = torch.cuda.Stream(device=self.device)
-            side.wait_stream(torch.cuda.current_stream(self.device))
-            g = torch.cuda.CUDAGraph()
-            with capture_guard(), torch.cuda.stream(side):
-                with torch.cuda.graph(g, stream=side):
-                    self._graph_call(ws)
-            torch.cuda.current_stream(self.device).wait_stream(side)
-            self._graph, self._graph_key = g, key
-        return self._graph, ws
+            self._graph, self._graph_key = self._capture(ws, 1), key
+            self._graphs_unrolled = {}
+        if unroll == 1:
+            return self._graph, ws
+        g = self._graphs_unrolled.get(unroll)
+        if g is None:
+            g = self._graphs_unrolled[unroll] = self._capture(ws, unroll)
+        return g, ws
 
     def _run_graph(self, n_iter, log_time):
-        """``n_iter`` iterations as replays of one captured iteration: the Philox
-        call counter and the history row advance on the device."""
-        g, ws = self._graph_for(n_iter)
+        """``n_iter`` iterations as replays of captured iterations: the Philox
+        call counter and the history row advance on the device.  Without
+        per-iteration logging, up to GRAPH_UNROLL iterations go into one replay
+        (one graph launch, and one host call, instead of several)."""
+        unroll = 1 if self._verbose else max(1, min(n_iter, GRAPH_UNROLL))
+        g1, ws = self._graph_for(n_iter)
+        gu = self._graph_for(n_iter, unroll)[0] if unroll > 1 else g1
         # the start counters (call, iteration) as one 64-bit device fill: asynchronous,
         # and no pinned host buffer (whose release could record events on a stream
         # while another stream captures)
         start = np.array([self._call_ctr & 0xFFFFFFFF, self._it], dtype=np.uint32).view(np.int64)
         ws["counters"].view(torch.int64).fill_(int(start[0]))
-        for i in range(n_iter):
-            if log_time:
+        if self._verbose:
+            for i in range(n_iter):
                 t0 = time.time()
-            g.replay()
-            self._history.append([None, None, None])
-            if self._verbose:
+                g1.replay()
+                self._history.append([None, None, None])
                 row = ws["history"][self._it + i].cpu().numpy()
                 time_str = f"(took {time.time() - t0:.5f} s)" if log_time else ""
                 logger.info(print_iteration(i, float(row[0]), float(row[1]), extra=time_str))
+        else:
+            full, rest = divmod(n_iter, unroll)
+            for _ in range(full):
+                gu.replay()
+            for _ in range(rest):
+                g1.replay()
+            self._history.extend([None, None, None] for _ in range(n_iter))
         self._call_ctr += n_iter
         self._it += n_iter
 
