@@ -626,10 +626,10 @@ def injected_run(dev, n_events, K, W, seed=11):
 
 def sampler_run(dev, n_events, K, W, seed=3):
     """The sampler API (VEGAS as a random-number generator): on a trained
-    8-D grid, ``generate_random_array(n)`` writes x (8 floats) and the weight
-    (1 float) of every event to HBM -- one map kernel launch plus the weight
-    normalisation.  ``value`` is through the public call; the roofline is the
-    map kernel alone (36 bytes written per event)."""
+    8-D grid, ``generate_random_array(n)`` writes x (8 floats) and the
+    normalised weight (1 float) of every event to HBM -- one map kernel launch.
+    ``value`` is through the public call; the roofline is the map kernel alone
+    (36 bytes written per event)."""
     import torch
 
     from vegasflow_gb300 import VegasFlow, integrands
