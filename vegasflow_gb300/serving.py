@@ -424,7 +424,11 @@ class VegasServer:
                 "events": int(sum(r.n_events for r in act))}
 
     def _prep_key(self, act, stream):
-        return (tuple(r.rid for r in act), stream.value, self.partials.data_ptr(), self._queue.data_ptr())
+        """Everything the step's tables and launch arguments are built from: per
+        request (in launch order) its stream id, slot, event and dimension counts
+        and program, and the buffers the arguments point into."""
+        reqs = tuple((r.rid, r.slot, r.n_events, r.n_dim, r.program or r.integrand.integrand_id) for r in act)
+        return (reqs, stream.value, self.partials.data_ptr(), self._queue.data_ptr())
 
     def step(self, now_fn):
         """Advance every active request by one iteration, then retire finished ones."""
