@@ -559,7 +559,7 @@ def f32_weight_prescale(c1):
     return max(-100, min(100, k))
 
 
-def vegas_map_f32_words(words, divisions, xjac):
+def vegas_map_f32_words(words, divisions, xjac, xmin=None, xdelta=None):
     """fp32 form of the importance map on one 32-bit Philox word per dimension
     (the fused sampler's and the map kernel's draw, no integration limits).
 
@@ -573,7 +573,11 @@ def vegas_map_f32_words(words, divisions, xjac):
     lo + delta (1 - frac(50 u)), the reference's lo + delta frac.  The weight is
     2^k C1_0 C1_1 ... C1_{D-1} in float32 left to right (k from
     ``f32_weight_prescale``) times the float32 constant
-    ``(-1)^D xjac 50^D 2^-k`` (its float64 product rounded once).
+    ``(-1)^D xjac 50^D 2^-k`` (its float64 product rounded once).  With
+    integration limits (monte_carlo.py:169-176, 270-273) the cell's affine
+    coefficients are ``c0 = fma64(lo - delta, xdelta, xmin)`` and
+    ``c1 = delta xdelta`` before the table is formed, so x is in the limits'
+    box and the weight carries the volume.
     Returns (ind int32, x float32, w float32)."""
     from fractions import Fraction
     words = np.asarray(words, dtype=np.uint32)
@@ -587,6 +591,12 @@ def vegas_map_f32_words(words, divisions, xjac):
     lo = g[:, :-1]
     c1 = g[:, 1:] - lo
     c0 = lo - c1
+    if xmin is not None:
+        xmin = np.asarray(xmin, dtype=np.float64)
+        xdelta = np.asarray(xdelta, dtype=np.float64)
+        c0 = np.array([[float(Fraction(float(a)) * Fraction(float(xdelta[d])) + Fraction(float(xmin[d])))
+                        for a in c0[d]] for d in range(n_dim)])
+        c1 = c1 * xdelta[:, None]
     # fma64(3, c1, c0) rounded to float64 once (exact rational sum, nearest-even)
     big = np.array([[float(Fraction(3) * Fraction(float(b)) + Fraction(float(a))) for a, b in zip(ra, rb)]
                     for ra, rb in zip(c0, c1)])

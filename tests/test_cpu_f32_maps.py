@@ -53,6 +53,26 @@ def test_vegas_f32_bins_are_the_reference_bins():
         np.testing.assert_allclose(w, w64, rtol=(n_dim + 2) * 2.0 ** -23)
 
 
+def test_vegas_f32_map_with_limits():
+    """With integration limits x lies in the limits' image of its bin and the
+    weight carries the box's volume, within float32 rounding."""
+    rng = np.random.default_rng(4)
+    n_dim = 3
+    grid = np.stack([oracle.refine_grid_per_dimension(rng.random(50) ** 2, np.linspace(0, 1, 51))
+                     for _ in range(n_dim)])
+    xmin = np.array([-1.0, 0.25, 3.0])
+    xdelta = np.array([4.0, 3.25, 0.5])
+    words = oracle.philox_words(9, 2, 0, 5000, n_dim)
+    ind, x, w = oracle.vegas_map_f32_words(words, grid, 1.0 / 5000, xmin, xdelta)
+    ind0, _, _ = oracle.vegas_map_f32_words(words, grid, 1.0 / 5000)
+    np.testing.assert_array_equal(ind, ind0)  # the bins do not depend on the limits
+    lo = xmin + np.take_along_axis(grid, ind.T, axis=1).T * xdelta
+    hi = xmin + np.take_along_axis(grid, ind.T + 1, axis=1).T * xdelta
+    assert np.all(x >= lo - 1e-5) and np.all(x <= hi + 1e-5)
+    w64 = np.prod((hi - lo), axis=1) * 50.0 ** n_dim / 5000
+    np.testing.assert_allclose(w, w64, rtol=(n_dim + 4) * 2.0 ** -23)
+
+
 def test_f32_weight_prescale_keeps_16d_weights_in_range():
     """Narrow bins at 16 dimensions: prod_d delta underflows float32 without the
     power-of-two prescale, with it the weight keeps float32 precision."""

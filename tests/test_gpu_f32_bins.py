@@ -10,8 +10,8 @@ vflow.py:93-126, :67 and vflowplus.py:46-80, both pinned to the reference's
 own fixtures), and for injected float64 uniforms the reference's bins of those
 uniforms.  Bar: ``assert_array_equal`` on every index.  The map kernel of the
 sampler API (the same draw without an integrand) is also checked for its
-points (within 1 float32 ulp of the oracle's one-rounding restatement) and
-weights (bit-exact)."""
+points and weights, bit for bit against the oracle's restatement, with and
+without integration limits."""
 
 import numpy as np
 import pytest
@@ -24,8 +24,8 @@ from vegasflow_gb300 import _native as nat
 pytestmark = pytest.mark.gpu
 
 
-def _trained(n_dim, n, integrand, seed=31, iters=3):
-    inst = VegasFlow(n_dim, n, verbose=False, precision="fp32", seed=seed)
+def _trained(n_dim, n, integrand, seed=31, iters=3, **limits):
+    inst = VegasFlow(n_dim, n, verbose=False, precision="fp32", seed=seed, **limits)
     inst.compile(integrand)
     inst.run_integration(iters)
     return inst
@@ -79,6 +79,26 @@ def test_map_kernel_points_and_weights_match_oracle(n_dim, with_ind):
     np.testing.assert_array_equal(w.cpu().numpy().view(np.uint32), w_o.view(np.uint32))
 
 
+@pytest.mark.parametrize("n_dim", [3, 8])
+def test_map_kernel_with_limits_matches_oracle(n_dim):
+    """Integration limits fold into the table (c0 = fma(lo - delta, xdelta, xmin),
+    c1 = delta xdelta): x in the limits' box and w with its volume, bit for bit."""
+    n, call = 500_003, 6
+    rng = np.random.default_rng(n_dim)
+    xmin = rng.uniform(-2.0, 1.0, n_dim)
+    xmax = xmin + rng.uniform(0.1, 4.0, n_dim)
+    inst = _trained(n_dim, n, integrands.prod(), xmin=list(xmin), xmax=list(xmax))
+    x = torch.empty((n, n_dim), dtype=torch.float32, device="cuda")
+    w = torch.empty(n, dtype=torch.float32, device="cuda")
+    inst._sample(n, 0, call, nat.VF_INT_NONE, None, False, False, x=x, w=w)
+    torch.cuda.synchronize()
+    words = oracle.philox_words(inst._seed, call, 0, n, n_dim)
+    grid = inst.divisions.cpu().numpy()
+    _, x_o, w_o = oracle.vegas_map_f32_words(words, grid, inst.xjac, inst._xmin_np, inst._xdelta_np)
+    np.testing.assert_array_equal(x.cpu().numpy().view(np.uint32), x_o.view(np.uint32))
+    np.testing.assert_array_equal(w.cpu().numpy().view(np.uint32), w_o.view(np.uint32))
+
+
 def _near_edge_uniforms(n_dim):
     """Uniforms a few float64 ulps around every bin edge 1 - k/50 (k = 1..49)
     and near the ends of the reference's range [1e-8, 1 - 1e-8)."""
@@ -99,7 +119,8 @@ def _near_edge_uniforms(n_dim):
 
 @pytest.mark.parametrize("n_dim,n,misalign", [(8, 10_000_000, False), (16, 1_000_000, False),
                                               (4, 1_000_000, False), (8, 1_000_000, True),
-                                              (5, 1_000_000, False)])
+                                              (5, 1_000_000, False), (1, 300_000, False),
+                                              (2, 300_000, False), (12, 1_000_000, False)])
 def test_injected_fused_bins_are_the_reference_bins(n_dim, n, misalign):
     """C2's injected mode (default_rng(11) through the TECH_CUT affine) with the
     near-edge uniforms first: the TMA path (D = 4, 8, 16 on an aligned array)
