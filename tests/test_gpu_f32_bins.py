@@ -56,20 +56,21 @@ def test_fused_sampler_bins_are_the_reference_bins(n_dim, which, offset):
     np.testing.assert_array_equal(ind.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("n_dim", [1, 3, 5, 8, 16])
+@pytest.mark.parametrize("n_dim,offset", [(1, 0), (3, 0), (5, 0), (8, 0), (16, 0), (8, (1 << 32) - 300_000)])
 @pytest.mark.parametrize("with_ind", [True, False])
-def test_map_kernel_points_and_weights_match_oracle(n_dim, with_ind):
+def test_map_kernel_points_and_weights_match_oracle(n_dim, offset, with_ind):
     """x, w (and bins) of the map kernel bit for bit against the oracle's
-    restatement; n is not a multiple of the 32-event tiles, so the last tile
-    takes the plain-store path."""
+    restatement; n is not a multiple of the warp tiles, so the last tile takes
+    the plain-store path; an event offset near 2^32 makes the counter's high
+    word change inside the launch."""
     n, call = 1_000_003, 5
     inst = _trained(n_dim, n, integrands.symgauss(0.2))
     x = torch.empty((n, n_dim), dtype=torch.float32, device="cuda")
     w = torch.empty(n, dtype=torch.float32, device="cuda")
     ind = torch.empty((n, n_dim), dtype=torch.int32, device="cuda") if with_ind else None
-    inst._sample(n, 0, call, nat.VF_INT_NONE, None, False, False, ind=ind, x=x, w=w)
+    inst._sample(n, offset, call, nat.VF_INT_NONE, None, False, False, ind=ind, x=x, w=w)
     torch.cuda.synchronize()
-    words = oracle.philox_words(inst._seed, call, 0, n, n_dim)
+    words = oracle.philox_words(inst._seed, call, offset, n, n_dim)
     grid = inst.divisions.cpu().numpy()
     ind_o, x_o, w_o = oracle.vegas_map_f32_words(words, grid, inst.xjac)
     if with_ind:
