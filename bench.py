@@ -58,6 +58,10 @@ CPU_BASELINE_STEPS = 8  # timed CPU iterations of the GPU arm's cpu_baseline (~1
 #   histogram: address + shared atomic per dim                             2 x 8 =   16
 #   loop control                                                                        3
 INSTR_PER_EVENT_FP32_D8 = 208
+# Of those, the 32 x 32 -> 64-bit multiplies (the FMA-heavy pipe, a quarter of
+# the FFMA rate on this part): 2 per Philox round x 10 rounds x 2 blocks, and
+# one per dimension for the bin map p = 50 w + 25.
+WIDE_MUL_PER_EVENT_FP32_D8 = 2 * 10 * 2 + 8
 
 # Injected-uniform mode (uniforms streamed from HBM): algorithmic bytes per event
 # = n_dim float64 uniforms.
@@ -477,6 +481,18 @@ def main():
         torch.cuda.synchronize()
         probe_s = pa.elapsed_time(pb) / 1e3
         issue_peak = probe_blocks * 256 * fpt.value / 32 / probe_s  # warp instructions / s
+        # the FMA-heavy pipe's rate for the 64-bit multiplies of Philox and the bin map
+        mul_buf = probe_buf.view(torch.int32)
+        mpt = ctypes.c_longlong(0)
+        for _ in range(2):
+            nat.check(lib.vf_widemul_probe(nat.ptr(mul_buf), probe_blocks, 4000, ctypes.byref(mpt),
+                                           nat.stream_handle()))
+        pa.record(stream)
+        nat.check(lib.vf_widemul_probe(nat.ptr(mul_buf), probe_blocks, 4000, ctypes.byref(mpt),
+                                       nat.stream_handle()))
+        pb.record(stream)
+        torch.cuda.synchronize()
+        widemul_peak = probe_blocks * 256 * mpt.value / 32 / (pa.elapsed_time(pb) / 1e3)  # warp instr / s
 
         # end to end with host buffers: through the C-ABI as a plugin drives it
         # (the headline), and through the Python API
@@ -496,7 +512,6 @@ def main():
     value64 = events_all / total64
 
     samp_mean = float(s32.mean())
-    achieved = INSTR_PER_EVENT_FP32_D8 * args.events / 32 / samp_mean  # warp instr / s
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * total32 / K, "higher_is_better": True, "scaling": "weak",
@@ -511,15 +526,7 @@ def main():
         "fp64_plain": {"value": value64, "unit": "events/s", "ms_per_step": 1e3 * total64 / K,
                        "sampler_ms": 1e3 * float(s64.mean())},
         "fp32_over_fp64": value / value64,
-        "roofline": {"bound": "issue", "kernel": "vf_vegas_f32_kernel<8,SYMGAUSS,1024>",
-                     "achieved": achieved / 1e9, "peak": issue_peak / 1e9, "unit": "Gwarp-instr/s",
-                     "frac": achieved / issue_peak, "traffic": SAMPLER_DRAM_BYTES,
-                     "traffic_note": "DRAM bytes per launch (ncu dram__bytes_read.sum + "
-                                     "dram__bytes_write.sum on a 1e7-event launch); the kernel "
-                                     "streams no per-event data, so this does not grow with events",
-                     "per_event_instr": INSTR_PER_EVENT_FP32_D8,
-                     "peak_source": "measured in this run: vf_issue_probe (independent FFMA chains)",
-                     "sampler_ms": 1e3 * samp_mean},
+        "roofline": sampler_roofline(args.events / samp_mean, samp_mean, issue_peak, widemul_peak),
         "e2e": e2e,
         "e2e_python_api": e2e_api,
         "injected": injected,
@@ -545,6 +552,49 @@ def main():
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def sampler_roofline(events_per_s, sampler_s, issue_peak, widemul_peak):
+    """The headline kernel's roofline: the binding pipe of its per-event
+    instruction budget (the lower of the pipe bounds), both pipes measured in
+    this run.  `achieved` = the event's instructions on that pipe x events / 32
+    / sampler time, against the pipe's probe rate."""
+    bounds = pipe_bounds(events_per_s, issue_peak, widemul_peak)
+    b = bounds["binding"]
+    ops = bounds[b]["ops_per_event"]
+    peak = bounds[b]["peak_gwarp_instr_per_s"] * 1e9
+    achieved = ops * events_per_s / 32
+    names = {"issue": ("issue (warp-instruction issue rate)", "vf_issue_probe: independent FFMA chains"),
+             "fma_heavy_wide_multiplies": ("FMA-heavy pipe (64-bit integer multiplies of Philox and the bin map)",
+                                           "vf_widemul_probe: Philox-shaped multiply/XOR chains")}
+    return {"bound": names[b][0], "kernel": "vf_vegas_f32_kernel<8,SYMGAUSS,1024>",
+            "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "Gwarp-instr/s", "frac": achieved / peak,
+            "traffic": SAMPLER_DRAM_BYTES,
+            "traffic_note": "DRAM bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum on a "
+                            "1e7-event launch); the kernel streams no per-event data, so this does not grow "
+                            "with events",
+            "per_event_instr": ops,
+            "peak_source": "measured in this run: " + names[b][1],
+            "pipe_bounds": bounds,
+            "sampler_ms": 1e3 * sampler_s}
+
+
+def pipe_bounds(events_per_s, issue_peak, widemul_peak):
+    """The fused sampler's per-pipe bounds at D = 8, each from a rate measured
+    in this run: events/s if only that pipe limited it (its peak warp
+    instructions/s x 32 / the event's instructions on it), and the sampler's
+    fraction of each.  Issue: all 208 algorithmic instructions; the FMA-heavy
+    pipe: the 48 64-bit multiplies (40 in the two Philox blocks, 8 in the bin
+    map), at the rate of vf_widemul_probe."""
+    ev_s = events_per_s
+    out = {}
+    for name, peak, ops in (("issue", issue_peak, INSTR_PER_EVENT_FP32_D8),
+                            ("fma_heavy_wide_multiplies", widemul_peak, WIDE_MUL_PER_EVENT_FP32_D8)):
+        bound = peak * 32 / ops
+        out[name] = {"ops_per_event": ops, "peak_gwarp_instr_per_s": peak / 1e9,
+                     "bound_events_per_s": bound, "frac": ev_s / bound}
+    out["binding"] = min(("issue", "fma_heavy_wide_multiplies"), key=lambda k: out[k]["bound_events_per_s"])
+    return out
 
 
 def measured_hbm_peak():

@@ -388,6 +388,15 @@ int vf_tune_get(int key, int* value);
  * on an impossible value); *fma_per_thread receives 128 * iters.
  */
 int vf_issue_probe(float* out, int blocks, int iters, long long* fma_per_thread, void* stream);
+/*
+ * The same for the 64-bit integer multiplies of Philox4x32-10 and the integer
+ * bin map (the FMA-heavy pipe): each thread runs 128 * iters steps of eight
+ * independent chains shaped like a Philox round, one 32 x 32 -> 64-bit
+ * multiply and one three-input XOR per step; *mul_per_thread receives
+ * 128 * iters.  `out`: blocks * 256 unsigned ints (written only on an
+ * impossible value).
+ */
+int vf_widemul_probe(unsigned* out, int blocks, int iters, long long* mul_per_thread, void* stream);
 
 #ifdef __cplusplus
 }

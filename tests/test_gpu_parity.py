@@ -307,6 +307,30 @@ def test_float32_refinement_close_to_float64(spread, empty, scale):
     assert np.all(out[2][:, 0] == 0.0) and np.all(out[2][:, -1] == 1.0)
 
 
+def test_pipe_probes():
+    """The calibration probes of the fused sampler's roofline run and report their
+    work: FFMA chains (the issue rate) and Philox-shaped wide-multiply chains
+    (the FMA-heavy pipe), the latter slower per instruction on this part."""
+    import ctypes
+    lib = nat.load()
+    blocks = 152 * 4
+    buf = torch.empty(blocks * 256, dtype=torch.float32, device="cuda")
+    rates = {}
+    for name in ("vf_issue_probe", "vf_widemul_probe"):
+        per_thread = ctypes.c_longlong(0)
+        fn = getattr(lib, name)
+        nat.check(fn(nat.ptr(buf), blocks, 200, ctypes.byref(per_thread), nat.stream_handle()))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        nat.check(fn(nat.ptr(buf), blocks, 2000, ctypes.byref(per_thread), nat.stream_handle()))
+        b.record()
+        b.synchronize()
+        assert per_thread.value == 128 * 2000
+        rates[name] = blocks * 256 * per_thread.value / 32 / (a.elapsed_time(b) / 1e3)
+    assert rates["vf_issue_probe"] > rates["vf_widemul_probe"] > 0
+    assert lib.vf_widemul_probe(None, blocks, 10, None, None) == nat.VF_ERR_ARG
+
+
 def test_bounded_device_wait_reports_timeout():
     """The TMA path's bounded mbarrier wait, on a barrier nothing completes,
     gives up and sets VF_FLAG_TIMEOUT; the context stays usable afterwards."""

@@ -70,6 +70,7 @@ SIGNATURES = {
     "vf_refine_grid": [_P, _P, _I, _D, _P, _P],
     "vf_consume_array_into_indices": [_P, _P, _LL, _I, _P, _P, _P],
     "vf_issue_probe": [_P, _I, _I, _P, _P],
+    "vf_widemul_probe": [_P, _I, _I, _P, _P],
     "vf_vegas_iteration_static": [_I, _P, _I, _LL, _U64, _U32, _I, _P, _I, _P, _P, _P],
     "vf_philox_uniforms": [_U64, _U32, _U32, _LL, _LL, _I, _P, _P],
     "vf_plus_rows": [_I, _I, _I, _P],

@@ -38,6 +38,42 @@ extern "C" int vf_issue_probe(float* out, int blocks, int iters, long long* fma_
 
 namespace {
 
+// The same for the 64-bit integer multiply that Philox4x32-10 and the bin map
+// issue (the FMA-heavy pipe): eight independent chains per thread of the
+// Philox round's shape -- (hi, lo) = a * M, a' = hi ^ lo ^ k -- one wide
+// multiply and one three-input XOR (the ALU pipe) per step, so the wide
+// multiplies bound the chain's rate.
+__global__ void __launch_bounds__(256) vf_widemul_probe_kernel(unsigned* out, int iters) {
+  unsigned a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = threadIdx.x * 2654435761u + (unsigned)j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const unsigned long long p = (unsigned long long)a[j] * 0xD2511F53ull;
+        a[j] = (unsigned)(p >> 32) ^ (unsigned)p ^ 0x9E3779B9u;
+      }
+    }
+  }
+  unsigned s = 0u;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s ^= a[j];
+  if (s == 0x12345678u) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" int vf_widemul_probe(unsigned* out, int blocks, int iters, long long* mul_per_thread, void* stream) {
+  if (!out || blocks < 1 || iters < 1) return VF_ERR_ARG;
+  vf_widemul_probe_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(out, iters);
+  if (mul_per_thread) *mul_per_thread = 8LL * 16LL * iters;
+  return cudaGetLastError() == cudaSuccess ? VF_OK : VF_ERR_LAUNCH;
+}
+
+namespace {
+
 // The bounded wait of the TMA path, on a barrier that nothing completes: every
 // thread gives up after `polls` polls and the block reports it.
 __global__ void __launch_bounds__(64) vf_wait_selftest_kernel(int polls, int* flag) {
@@ -64,6 +100,7 @@ namespace vf {
 cudaError_t preload_probe_kernels() {
   cudaFuncAttributes attr;
   cudaError_t e = cudaFuncGetAttributes(&attr, vf_issue_probe_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_widemul_probe_kernel);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, vf_wait_selftest_kernel);
   return e;
 }
