@@ -35,7 +35,7 @@ __all__ = [
     "OracleVegas", "OraclePlain", "OraclePlus", "INTEGRANDS", "integrand_symgauss",
     "integrand_gauss_mu", "integrand_breit_wigner", "integrand_prod", "integrand_sum",
     "symgauss_exact", "gauss_mu_exact", "breit_wigner_exact", "threaded_vegas_iteration",
-    "uniforms_of_words", "plus_bins_from_words", "hypercube_points",
+    "uniforms_of_words", "plus_bins_from_words", "plus_map_f32_words", "hypercube_points",
     "fma_f32",
 ]
 
@@ -631,6 +631,36 @@ def plus_bins_from_words(words, points, n_strat):
     p = np.asarray(points, dtype=np.uint64)
     Q = ((p << np.uint64(32)) | w) * np.uint64(50) + np.uint64(25)
     return ((Q >> np.uint64(32)) // np.uint64(int(n_strat))).astype(np.int32)
+
+
+def plus_map_f32_words(words, points, n_strat, divisions):
+    """The fp32 VEGAS+ sampler's points (no integration limits): with
+    Q = 50 (p 2^32 + word) + 25, A = Q >> 32, R = Q mod 2^32, bin i = A div
+    n_strat and r = A mod n_strat (``plus_bins_from_words``), the fraction plus 1
+    is ``m = fl32(fl32(R 2^-32 + r) / n_strat + 1)`` with the division by a
+    float32 reciprocal and both steps fused multiply-adds, capped below 2, and
+    ``x = fl32(c1 m + c0)`` through the per-bin table ``c0 = f32(lo - delta)``,
+    ``c1 = f32(delta)`` (each rounded once from float64).  Returns x float32."""
+    w = np.asarray(words, dtype=np.uint64)
+    p = np.asarray(points, dtype=np.uint64)
+    ns = int(n_strat)
+    Q = ((p << np.uint64(32)) | w) * np.uint64(50) + np.uint64(25)
+    A = Q >> np.uint64(32)
+    R = (Q & _MASK32).astype(np.uint32)
+    i = (A // np.uint64(ns)).astype(np.int64)
+    r = (A - (A // np.uint64(ns)) * np.uint64(ns)).astype(np.float32)
+    inv_ns = np.float32(1.0) / np.float32(ns)
+    t = fma_f32(R.astype(np.float32), np.full(R.shape, np.float32(2.0 ** -32)), r)
+    m = fma_f32(t, np.full(t.shape, inv_ns), np.ones(t.shape, dtype=np.float32))
+    m = np.minimum(m, np.float32(1.99999988))
+    g = np.asarray(divisions, dtype=np.float64)
+    lo = g[:, :-1]
+    dl = g[:, 1:] - lo
+    c0 = (lo - dl).astype(np.float32)
+    c1 = dl.astype(np.float32)
+    c0e = np.take_along_axis(c0, i.T, axis=1).T
+    c1e = np.take_along_axis(c1, i.T, axis=1).T
+    return fma_f32(c1e, m, c0e)
 
 
 def plain_map_f32_words(words):

@@ -181,8 +181,12 @@ def test_plus_fp32_bins_are_the_reference_bins(n_dim, n_events, adaptive, which)
     h = np.repeat(np.arange(inst._n_hcubes), n_ev)
     pts = oracle.hypercube_points(inst._n_hcubes, inst._n_strat, n_dim)[h]
     np.testing.assert_array_equal(got, oracle.plus_bins_from_words(words, pts, inst._n_strat))
-    # the points: float32 through the per-bin table, within 2e-6 of the float64 map
-    assert np.max(np.abs(x.cpu().numpy().astype(np.float64) - x64)) < 2e-6
+    # the points: bit for bit against the oracle's float32 restatement, and within
+    # 2e-6 of the float64 map
+    xg = x.cpu().numpy()
+    np.testing.assert_array_equal(xg.view(np.uint32),
+                                  oracle.plus_map_f32_words(words, pts, inst._n_strat, grid).view(np.uint32))
+    assert np.max(np.abs(xg.astype(np.float64) - x64)) < 2e-6
 
 
 @pytest.mark.parametrize("n_dim,call,offset", [(1, 0, 0), (8, 3, 5), (11, (1 << 28) + 2, 1 << 33)])

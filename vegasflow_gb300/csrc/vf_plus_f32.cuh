@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel
     const double dl = a.grid[d * VF_EDGES + b + 1] - lo;
     double c0 = lo - dl, c1 = dl;
     if (limits) {
-      c0 = a.xmin[d] + c0 * a.xdelta[d];
+      c0 = __fma_rn(c0, a.xdelta[d], a.xmin[d]);
       c1 = c1 * a.xdelta[d];
     }
     cells[k] = make_float2((float)c0, (float)c1);
@@ -108,7 +108,8 @@ __global__ void __launch_bounds__(VF_THREADS, D <= 8 ? 4 : 2) vf_plus_f32_kernel
             if (i * ns > A) --i;
             if ((i + 1) * ns <= A) ++i;
             const u32 r = A - i * ns;
-            float m = 1.0f + fmaf((float)R, 2.3283064e-10f, (float)r) * inv_ns;
+            // m = 1 + fraction: (r + R 2^-32) / n_strat, two fused multiply-adds
+            float m = fmaf(fmaf((float)R, 2.3283064e-10f, (float)r), inv_ns, 1.0f);
             m = fminf(m, 1.99999988f);  // keep the fraction below 1 after rounding
             const float2 c = cells[d * VF_BINS + i];
             x[d] = fmaf(c.y, m, c.x);
