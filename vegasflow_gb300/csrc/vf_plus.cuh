@@ -125,6 +125,16 @@ __device__ __forceinline__ double plus_damp(double v, double beta) {
   return pow(v, beta / 2.0);
 }
 
+// The same in float32 (the fp32 form's reallocation, as the reference's float32
+// mode computes it).  NaN for v < 0, as powf.
+__device__ __forceinline__ float plus_damp_f32(float v, double beta) {
+  if (beta == 0.75) {
+    const float r = sqrtf(sqrtf(sqrtf(v)));
+    return r * r * r;
+  }
+  return powf(v, (float)(beta / 2.0));
+}
+
 #define VF_PEND_CLUSTER 8
 #define VF_PEND_THREADS 512
 #define VF_PEND_MAXC 4  // hypercubes per thread: up to 8 x 512 x 4 = 16384
@@ -174,6 +184,11 @@ vf_plus_iteration_end_kernel(const PlusEndArgs a) {
   const int hi = (int)((long long)H * (rank + 1) / VF_PEND_CLUSTER);
   const int C = (hi - lo + VF_PEND_THREADS - 1) / VF_PEND_THREADS;
   const int h0 = lo + t * C;
+  // the fp32 form (float32 refinement): the variance stays float64 (it cancels),
+  // its sigma term's division, the damped variance and the new counts are float32
+  // -- the reference's float32-mode arithmetic -- which takes ~35 of the ~45
+  // float64 instructions per hypercube off this cluster's critical path
+  const bool f32 = a.train == 2;
   double dmp[VF_PEND_MAXC];
   double r1 = 0.0, r2 = 0.0, r3 = 0.0;
 #pragma unroll
@@ -186,40 +201,43 @@ vf_plus_iteration_end_kernel(const PlusEndArgs a) {
       const double var = __dsub_rn(__dmul_rn(a.ress2[h], nev), __dmul_rn(a.ress[h], a.ress[h]));
       if (a.arr_var) a.arr_var[h] = var;
       r1 += a.ress[h];
-      r2 += fmax(var, 0.0) / (nev - 1.0);
-      if (a.adaptive) {
-        dmp[j] = plus_damp(var, a.beta);
-        r3 += dmp[j];
+      if (f32) {
+        r2 += (double)((float)fmax(var, 0.0) / (float)(a.n_ev[h] - 1));
+        if (a.adaptive) {
+          dmp[j] = (double)plus_damp_f32((float)var, a.beta);
+          r3 += dmp[j];
+        }
+      } else {
+        r2 += fmax(var, 0.0) / (nev - 1.0);
+        if (a.adaptive) {
+          dmp[j] = plus_damp(var, a.beta);
+          r3 += dmp[j];
+        }
       }
     }
   }
-  __shared__ double wpart[3][VF_PEND_THREADS / 32];
+  // block sums in a fixed order: the threads' partials to shared memory, then
+  // warp k < 3 adds sum k (16 strided values per lane, then a butterfly).  Every
+  // float64 addition costs its SM sub-partition 64 cycles, so three warps on
+  // three sub-partitions (36 additions each) beat a butterfly in all 16 warps
+  // (15 additions each, four warps per sub-partition) plus a serial pass.
+  __shared__ double part[3][VF_PEND_THREADS];
   __shared__ double tot[3];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    r1 += __shfl_xor_sync(0xffffffffu, r1, o);
-    r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-    r3 += __shfl_xor_sync(0xffffffffu, r3, o);
-  }
-  if (lane == 0) {
-    wpart[0][warp] = r1;
-    wpart[1][warp] = r2;
-    wpart[2][warp] = r3;
-  }
+  part[0][t] = r1;
+  part[1][t] = r2;
+  part[2][t] = r3;
   __syncthreads();
-  if (t == 0) {
-    double b1 = 0.0, b2 = 0.0, b3 = 0.0;
-    for (int w = 0; w < VF_PEND_THREADS / 32; ++w) {
-      b1 += wpart[0][w];
-      b2 += wpart[1][w];
-      b3 += wpart[2][w];
-    }
-    tot[0] = b1;
-    tot[1] = b2;
-    tot[2] = b3;
+  if (warp < 3) {
+    double v = 0.0;
+#pragma unroll 4
+    for (int i = lane; i < VF_PEND_THREADS; i += 32) v += part[warp][i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) tot[warp] = v;
   }
   cluster.sync();
   __shared__ double all[3];  // the cluster's totals, added in rank order in every block
+  __shared__ float s_scale;  // the fp32 form's count scale N0 / 2 / sum d
   __shared__ double s_mean;
   __shared__ int s_it, s_room;  // the iteration index; whether its history row exists
   if (t == 0) {
@@ -233,6 +251,7 @@ vf_plus_iteration_end_kernel(const PlusEndArgs a) {
     all[0] = c1;
     all[1] = c2;
     all[2] = c3;
+    if (f32 && a.adaptive) s_scale = (float)(a.init_calls / 2.0 / c3);
     if (rank == 0) {
       const int it = a.iter_dev ? *a.iter_dev : a.iter;
       s_it = it;
@@ -282,8 +301,13 @@ vf_plus_iteration_end_kernel(const PlusEndArgs a) {
   for (int j = 0; j < VF_PEND_MAXC; ++j) {
     cnt[j] = 0;
     if (j < C && h0 + j < hi) {
-      const double nn = fmax((double)a.min_neval, dmp[j] * a.init_calls / 2.0 / sum_d);
-      cnt[j] = (long long)(int)nn;
+      if (f32) {
+        const float nn = fmaxf((float)a.min_neval, (float)dmp[j] * s_scale);  // one float32 product
+        cnt[j] = (long long)(int)nn;
+      } else {
+        const double nn = fmax((double)a.min_neval, dmp[j] * a.init_calls / 2.0 / sum_d);
+        cnt[j] = (long long)(int)nn;
+      }
       own += cnt[j];
     }
   }
