@@ -82,8 +82,12 @@ vf_iteration_end_kernel(const IterEndArgs a) {
     if (t == 0 && a.flags) atomicOr(a.flags, VF_FLAG_HISTORY_FULL);
     return;
   }
-  // ---- the sums, one output at a time
-  __shared__ double red[2][VF_END_THREADS / 32];
+  // ---- the sums, one output at a time: each thread's rows, then warp 0 adds
+  // res and warp 1 res2 over the threads' partials in a fixed order (float64
+  // additions cost an SM sub-partition 64 cycles each: two warps on two
+  // sub-partitions beat a butterfly in every warp plus a serial pass)
+  __shared__ double part[2][VF_END_THREADS];
+  __shared__ double tot[2];
   __shared__ double mean_sh, sums_sh[2];
   const int lane = t & 31, warp = t >> 5;
   for (int j = 0; j < K; ++j) {
@@ -92,22 +96,20 @@ vf_iteration_end_kernel(const IterEndArgs a) {
       s1 += a.partials[(long long)r * W + j];
       s2 += a.partials[(long long)r * W + K + j];
     }
+    part[0][t] = s1;
+    part[1][t] = s2;
+    __syncthreads();
+    if (warp < 2) {
+      double v = 0.0;
+#pragma unroll 4
+      for (int i = lane; i < (int)blockDim.x; i += 32) v += part[warp][i];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-    }
-    if (lane == 0) {
-      red[0][warp] = s1;
-      red[1][warp] = s2;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) tot[warp] = v;
     }
     __syncthreads();
     if (t == 0) {
-      double res = 0.0, res2 = 0.0;
-      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-        res += red[0][i];
-        res2 += red[1][i];
-      }
+      const double res = tot[0], res2 = tot[1];
       const double N = a.n_events;
       // vflow.py:437-438 (and plain.py:37-43, the same expression)
       const double err_tmp2 = __ddiv_rn(__dsub_rn(__dmul_rn(N, res2), __dmul_rn(res, res)), __dsub_rn(N, 1.0));
